@@ -1,0 +1,390 @@
+"""Benchmark: power spectra per second of the 512^3 CIC workload on GB300.
+
+One step = one pass of the hot path over one particle set: zero the grid,
+CIC deposit of 134,217,728 particles onto a 512^3 float32 grid, r2c FFT,
+window deconvolution, |delta_k|^2, Legendre ell=0,2,4 and integer-|k|
+binning, and the float64 per-bin sums back on the host (k3D, Pk[:,0:3],
+Nmodes3D) -- pyl_pk_particles, the reference's canonical
+MA -> delta/mean-1 -> Pk caller (Pk_snapshot.py:81-89) in one call.
+
+  value  spectra/s with the positions resident in HBM (device-timed).
+  e2e    the same metric through the public API power_spectrum() with the
+         positions in pinned host memory: every step copies them to the
+         device and reads the spectrum back.
+  roofline  the dominant kernel's algorithmic bytes per launch / its mean
+         CUDA-event duration, against the measured HBM copy bandwidth.
+  cpu_baseline  the reference's CPU path (oracle port: OpenMP atomic deposit
+         as MAS_c.c, scipy FFT on all cores as FFTW threads, the serial mode
+         loop of Pk) on a bounded sample of the same workload.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun (N > 1) every rank runs its own replica (no data exchange);
+value is the sum over ranks, timed as the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BOX = 1000.0
+METRIC = "P(k)/s @512^3 CIC"
+UNIT = "spectra/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dims", type=int, default=512)
+    ap.add_argument("--particles", type=int, default=512 ** 3)
+    ap.add_argument("--mas", default="CIC")
+    ap.add_argument("--axis", type=int, default=0)
+    ap.add_argument("--positions", default="uniform", choices=["uniform", "zeldovich"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=16,
+                    help="CPU baseline runs 1/this of the particles and of the mode loop")
+    return ap.parse_args()
+
+
+def workload(a):
+    return {
+        "workload": "%d^3 grid, %d %s particles, %s deposit + %s window, axis %d, "
+                    "BoxSize %g" % (a.dims, a.particles, a.positions, a.mas, a.mas, a.axis, BOX),
+        "dims": a.dims, "particles": a.particles, "positions": a.positions,
+        "mas": a.mas, "axis": a.axis, "box": BOX,
+        "l2": "inputs larger than L2 (positions %.2f GB, grid %.2f GB) -- no flush"
+              % (a.particles * 12 / 1e9, 4 * a.dims ** 3 / 1e9),
+    }
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -------------------------------------------------------------- roofline
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(stage, dims, n, weighted):
+    """Algorithmic HBM bytes per launch of each stage."""
+    h = dims // 2 + 1
+    real = 4 * dims ** 3
+    half = 8 * dims * dims * h
+    return {
+        "deposit": n * (12 + (4 if weighted else 0)) + real,   # read particles, write grid once
+        "fft_z": real + half,                                   # read real grid, write half-complex
+        "fft_y": 2 * half,                                      # read + write
+        "pk_x": half,                                           # read only (spectrum not stored)
+        "zero": real,
+    }.get(stage)
+
+
+def traffic_table():
+    """dram bytes per launch per stage from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            line = line.split("#")[0].split()
+            if len(line) >= 3:
+                out[(line[0], line[1])] = float(line[2])
+    return out
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(a, pos_np, threads):
+    """Reference CPU path on a bounded sample: returns seconds per spectrum
+    (extrapolated) and a description."""
+    import numpy as np
+    from oracle import oracle as orc
+    dims, S = a.dims, a.cpu_sample
+    n = pos_np.shape[0]
+    ns = n // S
+    grid = np.zeros((dims,) * 3, np.float32)
+    t0 = time.perf_counter()
+    orc.deposit_omp(a.mas, pos_np[:ns], grid, BOX, threads=threads)
+    t_dep = (time.perf_counter() - t0) * S
+    # the sampled grid stands in for the full one in the steps below
+    t0 = time.perf_counter()
+    grid /= np.mean(grid, dtype=np.float64)
+    grid -= 1.0
+    t_norm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dk = orc.FFT3Dr_f(grid, threads)
+    t_fft = time.perf_counter() - t0
+    rows = max(1, dims // S)
+    t0 = time.perf_counter()
+    orc.Pk(None, BOX, axis=a.axis, MAS=a.mas, delta_k=dk, rows=(0, rows))
+    t_bin = (time.perf_counter() - t0) * dims / rows
+    total = t_dep + t_norm + t_fft + t_bin
+    desc = ("oracle port on %d threads: OpenMP atomic deposit of 1/%d of the particles "
+            "(x%d), overdensity + scipy r2c FFT of the full grid, serial mode loop over "
+            "%d of %d kx planes (x%d); per-spectrum %.2f s = deposit %.2f + norm %.2f + "
+            "fft %.2f + bin %.2f" % (threads, S, S, rows, dims, dims // rows, total, t_dep,
+                                     t_norm, t_fft, t_bin))
+    return total, desc
+
+
+def host_positions(a, seed=1234):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    pos = rng.random((a.particles, 3), dtype=np.float32)
+    pos *= np.float32(BOX)
+    np.minimum(pos, np.nextafter(np.float32(BOX), np.float32(0)), out=pos)
+    return pos
+
+
+# ----------------------------------------------------------------- arms
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    pos = host_positions(a)
+    times = []
+    desc = ""
+    for i in range(a.warmup + a.steps):
+        t, desc = cpu_sample(a, pos, threads)
+        if i >= a.warmup:
+            times.append(t)
+    sec = sum(times) / len(times)
+    value = 1.0 / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform positions)",
+        "config": workload(a),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from pylians3_gb300 import build_native
+    build_native.build()
+    import pylians3_gb300 as P
+    from pylians3_gb300 import _native, synth
+    from pylians3_gb300.Pk_library import _Outputs, MAS_function
+    import ctypes
+
+    ctx = _native.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    if a.positions == "uniform":
+        pos = synth.uniform(a.particles, BOX, seed=1234 + rank)
+    else:
+        pos = synth.zeldovich(a.dims, BOX, sigma=3.0, seed=1234 + rank)
+        a.particles = pos.shape[0]
+    torch.cuda.synchronize()
+    out = _Outputs(a.dims, 0)
+    mas = _native.MAS_CODE[a.mas]
+    win = MAS_function(a.mas)
+
+    def step():
+        rc = ctx.lib.pyl_pk_particles(ctx.ptr, ctypes.c_void_p(pos.data_ptr()), a.particles,
+                                      None, a.dims, ctypes.c_float(BOX), mas, a.axis, win, 0,
+                                      ctypes.byref(out.struct), _native.PYL_DEVICE_PTRS)
+        ctx.check(rc)
+
+    for _ in range(a.warmup):
+        step()
+    ctx.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+        ctx.synchronize()
+
+    clocks = ClockSampler(local)
+    barrier()
+    ctx.stage_times(reset=True)
+    ctx.set_timing(True)
+    l0 = ctx.launches()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    launches = ctx.launches() - l0
+    stages = ctx.stage_times(reset=True)
+    ctx.set_timing(False)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / a.steps
+    value = world * a.steps / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    kern = {k: v for k, v in stages.items() if k not in ("h2d", "d2h")}
+    dom = max(kern, key=lambda k: kern[k][0])
+    dom_ms = kern[dom][0] / kern[dom][1]
+    algo = stage_bytes(dom, a.dims, a.particles, False)
+    achieved = algo / (dom_ms / 1e3) / 1e9
+    tr = traffic_table().get((dom, "%s_%d_%s" % (a.mas, a.dims, a.positions)))
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+            if peak_kind == "measured" else "fallback 6.8 TB/s",
+            "traffic": tr, "algorithmic_bytes_per_launch": algo, "ms_per_launch": dom_ms}
+    h = a.dims // 2 + 1
+    pipe_bytes = (a.particles * 12 + 4 * a.dims ** 3 + 4 * a.dims ** 3 + 2 * 8 * a.dims ** 2 * h)
+    stage_ms = {k: v[0] / a.steps for k, v in stages.items()}
+
+    # ---- end to end through the public API with pinned host positions
+    e2e = None
+    if not a.no_e2e:
+        host = P.pinned_empty((a.particles, 3), np.float32)
+        host[...] = pos.cpu().numpy()
+        for _ in range(2):
+            P.power_spectrum(host, a.dims, BOX, a.mas, axis=a.axis, ctx=ctx)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            P.power_spectrum(host, a.dims, BOX, a.mas, axis=a.axis, ctx=ctx)
+        t1 = time.perf_counter()
+        sec = t1 - t0
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([sec], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            sec = float(t.item())
+        kmax = _native.pk_sizes(a.dims)[0]
+        e2e = {"value": world * a.steps / sec, "unit": UNIT,
+               "h2d_bytes_per_step": a.particles * 12,
+               "d2h_bytes_per_step": 8 * (5 * (kmax + 1)),
+               "ms_per_step": sec / a.steps * 1e3}
+        del host
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        from oracle import oracle as orc
+        orc.build()
+        threads = os.cpu_count() or 1
+        pos_np = pos.cpu().numpy()
+        cpu_sample(a, pos_np, threads)   # warm-up (page faults, thread pools)
+        t, desc = cpu_sample(a, pos_np, threads)
+        cpu = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded %s positions, generated on the device)"
+                                     % a.positions,
+            "config": workload(a), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk, "gpu_launches": launches,
+            "stages_ms_per_step": stage_ms,
+            "pipeline_algorithmic_bytes": pipe_bytes,
+            "pipeline_frac": pipe_bytes / (ms_step / 1e3) / 1e9 / peak,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

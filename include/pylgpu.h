@@ -1,0 +1,167 @@
+/*
+ * pylgpu.h -- C ABI of libpylgpu.so, the GB300 (sm_103a) implementation of
+ * Pylians3's density-field + power-spectrum hot path.
+ *
+ * Conventions
+ *   - Every entry point returns 0 (PYL_OK) or a negative pyl_status; no
+ *     exception or exit() crosses the ABI.  pyl_last_error() gives the text.
+ *   - Plain pointers and sizes only.  With PYL_DEVICE_PTRS the array
+ *     arguments are device pointers (e.g. torch CUDA tensors, zero copy);
+ *     otherwise they are host pointers (pinned host memory copies fastest,
+ *     see pyl_host_alloc) and the library stages them through device memory.
+ *   - Arrays are C-contiguous: positions (n, coord) float32, grids
+ *     (dims, dims, dims) float32 (2D: (dims, dims)), spectra float64.
+ *   - Work is issued on the context's stream.  Calls with host outputs return
+ *     after the results are on the host; calls with device outputs return
+ *     once the work is enqueued (pyl_synchronize waits for it).
+ *   - A context is used by one host thread at a time, except the serving
+ *     calls (pyl_srv_*), which are thread safe.
+ *
+ * The reference interface each entry point replaces is cited beside it,
+ * as path:line in the Pylians3 source tree.
+ */
+#ifndef PYLGPU_H
+#define PYLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PYL_OK = 0,
+    PYL_ERR_ARG = -1,         /* bad argument (shape, MAS, size)            */
+    PYL_ERR_CUDA = -2,        /* a CUDA runtime call failed                  */
+    PYL_ERR_OOM = -3,         /* device or pinned allocation failed          */
+    PYL_ERR_MODES = -4,       /* mode-count self check failed (Pk :87-99)    */
+    PYL_ERR_TIMEOUT = -5,     /* a bounded wait gave up                      */
+    PYL_ERR_BUDGET = -6,      /* request larger than the HBM budget          */
+    PYL_ERR_UNSUPPORTED = -7, /* size or option this build does not handle   */
+    PYL_ERR_STATE = -8        /* call made in the wrong state                */
+} pyl_status;
+
+/* Mass-assignment schemes; the numbering is the reference's MAS_index
+ * (library/Pk_library/Pk_library.pyx:72-78): anything else = no window.  */
+enum { PYL_MAS_NONE = 0, PYL_MAS_NGP = 1, PYL_MAS_CIC = 2, PYL_MAS_TSC = 3,
+       PYL_MAS_PCS = 4 };
+
+/* flags */
+#define PYL_DEVICE_PTRS  0x01  /* array arguments are device pointers          */
+#define PYL_COMPENSATED  0x02  /* deposit: two-sum compensated accumulation    */
+#define PYL_DEPOSIT_ATOMIC 0x04 /* deposit: force the unsorted global-atomic path */
+#define PYL_DEPOSIT_SORTED 0x08 /* deposit: force the tile-sorted shared path  */
+
+/* Which Pk outputs to compute (bit mask); the 3D multipoles always are.   */
+#define PYL_PK_3D     0x00
+#define PYL_PK_1D     0x01     /* k1D, Pk1D, Nmodes1D                        */
+#define PYL_PK_2D     0x02     /* kpar, kper, Pk2D, Nmodes2D                 */
+#define PYL_PK_PHASE  0x04     /* Pkphase                                    */
+#define PYL_PK_ALL    0x07
+
+typedef struct pyl_ctx pyl_ctx;
+
+/* ---------------------------------------------------------------- context */
+/* device: CUDA ordinal; stream: a cudaStream_t to issue on, or NULL for a
+ * stream owned by the context.                                             */
+int pyl_ctx_create(pyl_ctx **out, int device, void *stream);
+int pyl_ctx_destroy(pyl_ctx *ctx);
+int pyl_ctx_set_stream(pyl_ctx *ctx, void *stream);
+/* The cudaStream_t the context issues on.                                  */
+int pyl_ctx_get_stream(const pyl_ctx *ctx, void **stream);
+int pyl_synchronize(pyl_ctx *ctx);
+const char *pyl_last_error(const pyl_ctx *ctx);
+/* Device bytes currently held by the context's workspaces and plans.      */
+int pyl_ctx_workspace_bytes(const pyl_ctx *ctx, size_t *bytes);
+/* Free cached workspaces and plans (they are rebuilt on demand).          */
+int pyl_ctx_trim(pyl_ctx *ctx);
+/* Number of kernel launches this context has issued (for accounting).     */
+int pyl_ctx_launch_count(const pyl_ctx *ctx, int64_t *count);
+/* Stage timing with CUDA events on the context stream (off by default).
+ * pyl_ctx_stage_times waits for recorded events, writes the accumulated
+ * milliseconds and launch counts of the first n stages (names from
+ * pyl_stage_name) and returns the number of stages; reset != 0 clears them. */
+int pyl_ctx_set_timing(pyl_ctx *ctx, int on);
+int pyl_ctx_stage_times(pyl_ctx *ctx, double *ms, int64_t *counts, int n, int reset);
+const char *pyl_stage_name(int stage);
+
+/* Pinned host memory (cudaHostAlloc) for fast host<->device staging.     */
+int pyl_host_alloc(void **ptr, size_t bytes);
+int pyl_host_free(void *ptr);
+
+/* ------------------------------------------------------ mass assignment */
+/* Deposit n particles onto grid with scheme mas, ACCUMULATING into grid
+ * (grid += ...), as MA does.  coord = 3: grid (dims,dims,dims);
+ * coord = 2: grid (dims,dims) -- the reference's expand_dims path -- and,
+ * when renormalize_2D != 0, the whole grid is then divided by 2/3/4 for
+ * CIC/TSC/PCS.  W (nullable) holds one weight per particle.
+ * Replaces: MA            library/MAS_library/MAS_library.pyx:57-112
+ *           NGP..PCSW     library/MAS_library/MAS_library.pyx:123-545
+ *           NGP..PCS (C)  library/MAS_library/MAS_c.h:3-10 (MAS_c.c:8-266) */
+int pyl_ma(pyl_ctx *ctx, const float *pos, int64_t n, int coord,
+           const float *W, float *grid, int dims, float BoxSize, int mas,
+           int renormalize_2D, int flags);
+
+/* Same deposit into a float64 grid (accumulated with float64 atomics; the
+ * per-tap weight is still the float32 product, as in the reference).
+ * Replaces: NGPW_d        library/MAS_library/MAS_library.pyx:338-358
+ *           CICW_d        library/MAS_library/MAS_library.pyx:229-266
+ * (any scheme and coord are accepted; renormalize_2D as pyl_ma).          */
+int pyl_ma_f64(pyl_ctx *ctx, const float *pos, int64_t n, int coord,
+               const float *W, double *grid, int dims, float BoxSize, int mas,
+               int renormalize_2D, int flags);
+
+/* ----------------------------------------------------------------- FFTs */
+/* r2c over all three axes, unnormalised; out is (dims,dims,dims/2+1)
+ * complex64 (interleaved float pairs).
+ * Replaces: FFT3Dr_f  library/Pk_library/Pk_library.pyx:117-130          */
+int pyl_fft_r2c(pyl_ctx *ctx, const float *in, float *out, int dims, int flags);
+/* c2r over all three axes, normalised by 1/dims^3 (pyFFTW's default).
+ * Replaces: IFFT3Dr_f library/Pk_library/Pk_library.pyx:149-162          */
+int pyl_fft_c2r(pyl_ctx *ctx, const float *in, float *out, int dims, int flags);
+
+/* -------------------------------------------------------- power spectrum */
+/* Output arrays, finalised exactly as class Pk leaves them (DC bin dropped,
+ * units applied, :384-418).  Sizes, with middle = dims/2:
+ *   kmax     = int(sqrt(3*middle^2)), kmax_par = middle,
+ *   kmax_per = int(sqrt(2*middle^2))
+ *   k3D, Nmodes3D, Pkphase : kmax entries;  Pk : kmax*3 (row-major [k][ell])
+ *   k1D, Pk1D, Nmodes1D    : kmax_par entries
+ *   kpar, kper, Pk2D, Nmodes2D : (kmax_par+1)*(kmax_per+1) entries
+ * Pointers of outputs not requested by `what` may be NULL.  All host memory. */
+typedef struct {
+    double *k3D, *Pk, *Nmodes3D;
+    double *k1D, *Pk1D, *Nmodes1D;
+    double *kpar, *kper, *Pk2D, *Nmodes2D;
+    double *Pkphase;
+} pyl_pk_out;
+
+/* Sizes of the output arrays for a grid of dims^3.                         */
+int pyl_pk_sizes(int dims, int *kmax, int *kmax_par, int *kmax_per);
+
+/* Power spectrum of an overdensity grid delta (dims^3 float32; not modified).
+ * mas is the window to deconvolve (PYL_MAS_*; other values: none).  axis is
+ * the line of sight (0, 1, 2; other values behave as 2, as in the
+ * reference).  Returns PYL_ERR_MODES when the mode count check fails.
+ * Replaces: class Pk  library/Pk_library/Pk_library.pyx:263-418          */
+int pyl_pk(pyl_ctx *ctx, const float *delta, int dims, double BoxSize,
+           int axis, int mas, int what, pyl_pk_out *out, int flags);
+
+/* Particles to spectrum in one call: zero a resident grid, deposit with
+ * mas_deposit, form delta = rho/mean - 1 (mean = grid mean, as the
+ * reference's callers compute it), and run Pk with window mas_window.  The
+ * overdensity step is folded into the spectrum (P(k!=0) of rho/mean - 1 is
+ * P(k) of rho divided by mean^2) so no extra pass over the grid is made.
+ * Replaces the canonical caller Pk_comp
+ *           library/Pk_library/Pk_snapshot.py:81-89
+ * (MA -> delta/=mean; delta-=1 -> Pk).                                    */
+int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n,
+                     const float *W, int dims, float BoxSize, int mas_deposit,
+                     int axis, int mas_window, int what, pyl_pk_out *out,
+                     int flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYLGPU_H */

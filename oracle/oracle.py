@@ -1,0 +1,272 @@
+"""CPU oracle for the Pylians3 density-field + power-spectrum hot path.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import this module, and only as the
+checker (or the timed CPU baseline) -- never as the thing measured or shipped.
+The product package ``pylians3_gb300`` never imports it.
+
+It restates, with the reference's floating-point types:
+  * ``MA`` / ``NGP`` ... ``PCSW``   -- library/MAS_library/MAS_library.pyx:57-545
+    (loops in oracle/pyl_oracle.c, dispatch and 2D renormalisation here, :57-112)
+  * ``deposit_omp``                -- library/MAS_library/MAS_c.c:8-266
+  * ``Pk``                         -- library/Pk_library/Pk_library.pyx:263-418
+    (mode loop in C; normalisation here, :384-418)
+  * ``FFT3Dr_f`` / ``IFFT3Dr_f``   -- Pk_library.pyx:117-130, :149-162.  The
+    reference calls pyFFTW (FFTW3f), which is not installed here; the
+    oracle uses scipy.fft (pocketfft) in float32 with the same conventions
+    (forward unnormalised, inverse normalised by 1/N^3).
+  * ``MA_f64`` / ``Pk_f64``        -- a float64 restatement (grid, FFT, window
+    and sums all in float64), the precision oracle.
+
+Parity of this restatement with the compiled reference is pinned by the
+golden vectors in tests/golden/ (see tests/test_oracle_golden.py).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_SO = os.path.join(_BUILD, "liborc.so")
+_SRC = os.path.join(_HERE, "pyl_oracle.c")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile pyl_oracle.c into oracle/_build/liborc.so (gcc, OpenMP).
+
+    ``-ffp-contract=off`` keeps every float operation separately rounded, as
+    the reference's C semantics state them.
+    """
+    os.makedirs(_BUILD, exist_ok=True)
+    if (not force and os.path.exists(_SO)
+            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+        return _SO
+    tmp = _SO + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-fno-fast-math", "-o", tmp, _SRC, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, _SO)
+    return _SO
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = ctypes.CDLL(_SO)
+    fp = ctypes.c_void_p
+    for name in ("orc_ngp", "orc_cic", "orc_tsc", "orc_pcs",
+                 "orc_ngp_d", "orc_cic_d", "orc_tsc_d", "orc_pcs_d"):
+        f = getattr(lib, name)
+        f.argtypes = [fp, ctypes.c_long, ctypes.c_int, fp, fp, ctypes.c_int,
+                      ctypes.c_float]
+        f.restype = None
+    lib.orc_deposit_omp.argtypes = [ctypes.c_int, fp, ctypes.c_long, fp, fp,
+                                    ctypes.c_int, ctypes.c_float, ctypes.c_int]
+    lib.orc_deposit_omp.restype = None
+    lib.orc_pk_bin.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_int] + [fp] * 9
+    lib.orc_pk_bin.restype = None
+    lib.orc_pk_bin_d.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 fp, fp, fp]
+    lib.orc_pk_bin_d.restype = None
+    lib.orc_num_threads.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+# --------------------------------------------------------------------------
+# Mass assignment (MAS_library.pyx:57-112)
+# --------------------------------------------------------------------------
+_MAS_FN = {"NGP": "orc_ngp", "CIC": "orc_cic", "TSC": "orc_tsc", "PCS": "orc_pcs"}
+
+
+def _deposit(MAS, pos, grid, BoxSize, W, f64=False):
+    lib = _load()
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    if W is not None:
+        W = np.ascontiguousarray(W, dtype=np.float32)
+    dims = grid.shape[0]
+    assert grid.flags.c_contiguous
+    fn = getattr(lib, _MAS_FN[MAS] + ("_d" if f64 else ""))
+    fn(pos.ctypes.data, pos.shape[0], pos.shape[1], _ptr(W), grid.ctypes.data,
+       dims, float(np.float32(BoxSize)))
+
+
+def MA(pos, number, BoxSize, MAS="CIC", W=None, verbose=False,
+       renormalize_2D=True):
+    """Restatement of MA (MAS_library.pyx:57-112): accumulates into `number`."""
+    coord, coord_aux = pos.shape[1], number.ndim
+    if coord != coord_aux:
+        print("pos have %d dimensions and the density %d!!!" % (coord, coord_aux))
+        sys.exit()
+    if MAS not in _MAS_FN:
+        print("option not valid!!!")
+        sys.exit()
+    f64 = number.dtype == np.float64
+    if coord == 3:
+        _deposit(MAS, pos, number, BoxSize, W, f64)
+    else:
+        number2 = np.expand_dims(number, axis=2)
+        _deposit(MAS, pos, number2, BoxSize, W, f64)
+        if renormalize_2D and MAS != "NGP":
+            number2 /= {"CIC": 2.0, "TSC": 3.0, "PCS": 4.0}[MAS]
+
+
+def MA_f64(pos, dims, BoxSize, MAS="CIC", W=None):
+    """Float64 grid deposit (precision oracle); weights computed as the
+    reference computes them, accumulation in float64 (cf. CICW_d :229-266)."""
+    grid = np.zeros((dims, dims, dims), np.float64)
+    _deposit(MAS, pos, grid, BoxSize, W, f64=True)
+    return grid
+
+
+def deposit_omp(MAS, pos, grid, BoxSize, W=None, threads=0):
+    """OpenMP atomic deposit (MAS_c.c:8-266), 3D; threads=0 uses all cores."""
+    lib = _load()
+    mas = {"NGP": 1, "CIC": 2, "TSC": 3, "PCS": 4}[MAS]
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    lib.orc_deposit_omp(mas, pos.ctypes.data, pos.shape[0], _ptr(W),
+                        grid.ctypes.data, grid.shape[0],
+                        float(np.float32(BoxSize)), int(threads))
+
+
+def num_threads() -> int:
+    return int(_load().orc_num_threads())
+
+
+# --------------------------------------------------------------------------
+# Power spectrum (Pk_library.pyx:56-130, 263-418)
+# --------------------------------------------------------------------------
+def frequencies(BoxSize, dims):
+    """Pk_library.pyx:56-61."""
+    kF = 2.0 * np.pi / BoxSize
+    middle = dims // 2
+    kN = middle * kF
+    kmax_par = middle
+    kmax_per = int(np.sqrt(middle ** 2 + middle ** 2))
+    kmax = int(np.sqrt(middle ** 2 + middle ** 2 + middle ** 2))
+    return kF, kN, kmax_par, kmax_per, kmax
+
+
+def MAS_function(MAS):
+    """Pk_library.pyx:72-78."""
+    return {"NGP": 1, "CIC": 2, "TSC": 3, "PCS": 4}.get(MAS, 0)
+
+
+def expected_modes(dims):
+    """Independent-mode count asserted by check_number_modes (:87-99)."""
+    own = 1 if dims % 2 == 1 else 8
+    return (dims ** 3 - own) // 2 + own
+
+
+def FFT3Dr_f(a, threads=1):
+    """r2c over (0,1,2), unnormalised, complex64 (Pk_library.pyx:117-130)."""
+    import scipy.fft as sf
+    return sf.rfftn(np.asarray(a, np.float32), axes=(0, 1, 2),
+                    workers=max(1, int(threads))).astype(np.complex64, copy=False)
+
+
+def IFFT3Dr_f(a, threads=1):
+    """c2r normalised by 1/N^3, float32 (Pk_library.pyx:149-162)."""
+    import scipy.fft as sf
+    dims = a.shape[0]
+    return sf.irfftn(np.asarray(a, np.complex64), s=(dims, dims, dims),
+                     axes=(0, 1, 2), workers=max(1, int(threads))
+                     ).astype(np.float32, copy=False)
+
+
+class Pk:
+    """Restatement of class Pk (Pk_library.pyx:263-418)."""
+
+    def __init__(self, delta, BoxSize, axis=2, MAS="CIC", threads=1,
+                 verbose=False, delta_k=None, rows=None):
+        lib = _load()
+        dims = len(delta) if delta is not None else delta_k.shape[0]
+        kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
+        MAS_index = MAS_function(MAS)
+        if delta_k is None:
+            delta_k = FFT3Dr_f(delta, threads)
+        delta_k = np.ascontiguousarray(delta_k, np.complex64)
+        k1D = np.zeros(kmax_par + 1)
+        Pk1D = np.zeros(kmax_par + 1)
+        N1D = np.zeros(kmax_par + 1)
+        Pk2D = np.zeros((kmax_par + 1) * (kmax_per + 1))
+        N2D = np.zeros((kmax_par + 1) * (kmax_per + 1))
+        k3D = np.zeros(kmax + 1)
+        Pk3D = np.zeros((kmax + 1, 3))
+        Pkphase = np.zeros(kmax + 1)
+        N3D = np.zeros(kmax + 1)
+        r0, r1 = (0, dims) if rows is None else rows
+        lib.orc_pk_bin(delta_k.ctypes.data, dims, int(axis), MAS_index, r0, r1,
+                       k1D.ctypes.data, Pk1D.ctypes.data, N1D.ctypes.data,
+                       Pk2D.ctypes.data, N2D.ctypes.data, k3D.ctypes.data,
+                       Pk3D.ctypes.data, Pkphase.ctypes.data, N3D.ctypes.data)
+        self.raw = dict(k3D=k3D.copy(), Pk3D=Pk3D.copy(), N3D=N3D.copy())
+        if rows is not None:          # bounded sample for timing: no finalisation
+            return
+        # --- normalisation, :384-418 ---
+        k1D, N1D, Pk1D = k1D[1:], N1D[1:], Pk1D[1:]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            Pk1D = Pk1D * (BoxSize / dims ** 2) ** 3
+            k1D = (k1D / N1D) * kF
+            kmaxper = np.sqrt(kN ** 2 - k1D ** 2)
+            Pk1D = Pk1D * (np.pi * kmaxper ** 2 / N1D) / (2.0 * np.pi) ** 2
+        self.k1D, self.Pk1D, self.Nmodes1D = k1D, Pk1D, N1D
+        kp = np.arange(kmax_par + 1)
+        kq = np.arange(kmax_per + 1)
+        self.kpar = np.tile(0.5 * (2 * kp + 1) * kF, kmax_per + 1)
+        self.kper = np.repeat(0.5 * (2 * kq + 1) * kF, kmax_par + 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            self.Pk2D = Pk2D * (BoxSize / dims ** 2) ** 3 / N2D
+        self.Nmodes2D = N2D
+        if int(np.sum(N3D)) != expected_modes(dims):
+            print("WARNING: Not all modes counted")
+            sys.exit()
+        k3D, N3D, Pk3D, Pkphase = k3D[1:], N3D[1:], Pk3D[1:, :], Pkphase[1:]
+        unit = (BoxSize / dims ** 2) ** 3
+        self.k3D = (k3D / N3D) * kF
+        P = np.empty_like(Pk3D)
+        P[:, 0] = (Pk3D[:, 0] / N3D) * unit
+        P[:, 1] = (Pk3D[:, 1] * 5.0 / N3D) * unit
+        P[:, 2] = (Pk3D[:, 2] * 9.0 / N3D) * unit
+        self.Pk = P
+        self.Pkphase = (Pkphase / N3D) * unit
+        self.Nmodes3D = N3D
+
+
+class Pk_f64:
+    """Float64 precision oracle: float64 FFT of a float64 grid, window and
+    sums in float64 (k3D, Pk[:,0:3], Nmodes3D as class Pk)."""
+
+    def __init__(self, delta, BoxSize, axis=2, MAS="CIC", threads=1):
+        import scipy.fft as sf
+        lib = _load()
+        dims = delta.shape[0]
+        kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
+        dk = np.ascontiguousarray(
+            sf.rfftn(np.asarray(delta, np.float64), axes=(0, 1, 2),
+                     workers=max(1, int(threads))), np.complex128)
+        k3D = np.zeros(kmax + 1)
+        Pk3D = np.zeros((kmax + 1, 3))
+        N3D = np.zeros(kmax + 1)
+        lib.orc_pk_bin_d(dk.ctypes.data, dims, int(axis), MAS_function(MAS),
+                         k3D.ctypes.data, Pk3D.ctypes.data, N3D.ctypes.data)
+        unit = (BoxSize / dims ** 2) ** 3
+        k3D, N3D, Pk3D = k3D[1:], N3D[1:], Pk3D[1:]
+        self.k3D = k3D / N3D * kF
+        self.Pk = np.stack([Pk3D[:, 0] / N3D * unit, Pk3D[:, 1] * 5.0 / N3D * unit,
+                            Pk3D[:, 2] * 9.0 / N3D * unit], axis=1)
+        self.Nmodes3D = N3D

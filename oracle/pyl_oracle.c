@@ -1,0 +1,413 @@
+/*
+ * CPU restatement of the Pylians3 density-field + power-spectrum hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the GPU library is
+ * checked against; it is compiled into oracle/_build/liborc.so and may only be
+ * loaded by tests/, __graft_entry__.smoke() and the CPU-baseline leg of
+ * bench.py.  The product path (pylians3_gb300) never links or calls it.
+ *
+ * Every routine restates one reference routine (paths relative to the Pylians3
+ * source tree) with the same floating-point types at each step:
+ *   orc_ngp / orc_cic / orc_tsc / orc_pcs  <- library/MAS_library/MAS_library.pyx
+ *        NGP :273-292, NGPW :305-325, CIC :123-166, CICW :179-216,
+ *        TSC :369-404, TSCW :417-452, PCS :463-497, PCSW :510-545
+ *   orc_*_d (float64 grid)                 <- NGPW_d :338-358, CICW_d :229-266
+ *        (extended here to TSC/PCS for the float64 precision oracle)
+ *   orc_deposit_omp                        <- library/MAS_library/MAS_c.c:8-266
+ *        (OpenMP particle loop with an atomic add per tap)
+ *   orc_pk_bin                             <- library/Pk_library/Pk_library.pyx:311-378
+ *        (the independent-mode loop of class Pk)
+ * Parity of this file with the compiled reference is pinned by the golden
+ * vectors under tests/golden/ (generated by tests/golden/make_golden.py from
+ * the reference compiled by oracle/build_ref.py).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Mass assignment.  pos is a C-contiguous (n, coord) float32 array, coord 2
+ * or 3; for coord == 2 the grid is (dims, dims, 1) as MA's expand_dims does
+ * (MAS_library.pyx:84-110) and the third axis keeps index 0 / weight 1.      */
+/* ------------------------------------------------------------------------ */
+
+#define DEPOSIT_BODY_CIC(GRID_T)                                                \
+    long i;                                                                     \
+    int axis;                                                                   \
+    float inv_cell_size = dims / box; /* int / float -> float, :135 */         \
+    float u[3] = {1.0f, 1.0f, 1.0f}, d[3] = {1.0f, 1.0f, 1.0f};                \
+    int iu[3] = {0, 0, 0}, id[3] = {0, 0, 0};                                  \
+    long sx = (long)dims * dz, sy = dz;                                         \
+    for (i = 0; i < n; i++) {                                                   \
+        float w = W ? W[i] : 1.0f;                                              \
+        for (axis = 0; axis < coord; axis++) {                                  \
+            float dist = pos[i * coord + axis] * inv_cell_size;                 \
+            u[axis] = dist - (float)(int)dist;                                  \
+            d[axis] = (float)(1.0 - (double)u[axis]);                           \
+            id[axis] = ((int)dist) % dims;                                      \
+            iu[axis] = (id[axis] + 1) % dims;                                   \
+        }                                                                       \
+        if (coord == 2) { id[2] = 0; iu[2] = 0; u[2] = 1.0f; d[2] = 1.0f; }     \
+        int zu = (coord == 2) ? 0 : iu[2];                                      \
+        if (W) {                                                                \
+            g[id[0]*sx + id[1]*sy + id[2]] += d[0]*d[1]*d[2]*w;                 \
+            g[id[0]*sx + id[1]*sy + zu]    += d[0]*d[1]*u[2]*w;                 \
+            g[id[0]*sx + iu[1]*sy + id[2]] += d[0]*u[1]*d[2]*w;                 \
+            g[id[0]*sx + iu[1]*sy + zu]    += d[0]*u[1]*u[2]*w;                 \
+            g[iu[0]*sx + id[1]*sy + id[2]] += u[0]*d[1]*d[2]*w;                 \
+            g[iu[0]*sx + id[1]*sy + zu]    += u[0]*d[1]*u[2]*w;                 \
+            g[iu[0]*sx + iu[1]*sy + id[2]] += u[0]*u[1]*d[2]*w;                 \
+            g[iu[0]*sx + iu[1]*sy + zu]    += u[0]*u[1]*u[2]*w;                 \
+        } else {                                                                \
+            g[id[0]*sx + id[1]*sy + id[2]] += d[0]*d[1]*d[2];                   \
+            g[id[0]*sx + id[1]*sy + zu]    += d[0]*d[1]*u[2];                   \
+            g[id[0]*sx + iu[1]*sy + id[2]] += d[0]*u[1]*d[2];                   \
+            g[id[0]*sx + iu[1]*sy + zu]    += d[0]*u[1]*u[2];                   \
+            g[iu[0]*sx + id[1]*sy + id[2]] += u[0]*d[1]*d[2];                   \
+            g[iu[0]*sx + id[1]*sy + zu]    += u[0]*d[1]*u[2];                   \
+            g[iu[0]*sx + iu[1]*sy + id[2]] += u[0]*u[1]*d[2];                   \
+            g[iu[0]*sx + iu[1]*sy + zu]    += u[0]*u[1]*u[2];                   \
+        }                                                                       \
+    }
+
+/* In 2D the reference passes number2 = expand_dims(number, 2) whose third
+ * extent is 1 (MAS_library.pyx:85); dz is that extent (dims in 3D, 1 in 2D). */
+
+void orc_cic(const float *pos, long n, int coord, const float *W, float *g,
+             int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_CIC(float)
+}
+
+void orc_cic_d(const float *pos, long n, int coord, const float *W, double *g,
+               int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_CIC(double)
+}
+
+#define DEPOSIT_BODY_NGP                                                        \
+    long i;                                                                     \
+    int axis;                                                                   \
+    float inv_cell_size = dims / box;                                           \
+    int idx[3] = {0, 0, 0};                                                     \
+    long sx = (long)dims * dz, sy = dz;                                         \
+    for (i = 0; i < n; i++) {                                                   \
+        for (axis = 0; axis < coord; axis++) {                                  \
+            /* float product, + 0.5 in double, truncation (:290) */             \
+            idx[axis] = (int)((double)(pos[i * coord + axis] * inv_cell_size)   \
+                              + 0.5);                                           \
+            idx[axis] = (idx[axis] + dims) % dims;                              \
+        }                                                                       \
+        g[idx[0]*sx + idx[1]*sy + idx[2]] += W ? W[i] : 1.0f;                   \
+    }
+
+void orc_ngp(const float *pos, long n, int coord, const float *W, float *g,
+             int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_NGP
+}
+
+void orc_ngp_d(const float *pos, long n, int coord, const float *W, double *g,
+               int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_NGP
+}
+
+/* TSC (:369-404) and PCS (:463-497): the window is built per axis with
+ * `minimum = (int)floor(dist - c)` in double, `diff = fabs(float(min+j+1) -
+ * dist)` in float and the polynomial in double, rounded to float on store.  */
+static inline void tsc_axis(float dist, int dims, int *index, float *C)
+{
+    int minimum = (int)floor((double)dist - 1.5);
+    for (int j = 0; j < 3; j++) {
+        index[j] = (minimum + j + 1 + dims) % dims;
+        float diff = (float)fabs((double)((float)(minimum + j + 1) - dist));
+        if (diff < 0.5)      C[j] = (float)(0.75 - (double)(diff * diff));
+        else if (diff < 1.5) C[j] = (float)(0.5 * (1.5 - diff) * (1.5 - diff));
+        else                 C[j] = 0.0f;
+    }
+}
+
+static inline void pcs_axis(float dist, int dims, int *index, float *C)
+{
+    int minimum = (int)floor((double)dist - 2.0);
+    for (int j = 0; j < 4; j++) {
+        index[j] = (minimum + j + 1 + dims) % dims;
+        float diff = (float)fabs((double)((float)(minimum + j + 1) - dist));
+        double dd = diff;
+        if (diff < 1.0)
+            C[j] = (float)((4.0 - 6.0 * dd * dd + 3.0 * dd * dd * dd) / 6.0);
+        else if (diff < 2.0)
+            C[j] = (float)((2.0 - dd) * (2.0 - dd) * (2.0 - dd) / 6.0);
+        else
+            C[j] = 0.0f;
+    }
+}
+
+#define DEPOSIT_BODY_SPLINE(NT, AXISFN)                                         \
+    long i;                                                                     \
+    int axis, l, m, q;                                                          \
+    float inv_cell_size = dims / box;                                           \
+    float C[3][NT];                                                             \
+    int index[3][NT];                                                           \
+    long sx = (long)dims * dz, sy = dz;                                         \
+    for (axis = 0; axis < 3; axis++)                                            \
+        for (l = 0; l < NT; l++) { C[axis][l] = 1.0f; index[axis][l] = 0; }     \
+    for (i = 0; i < n; i++) {                                                   \
+        for (axis = 0; axis < coord; axis++) {                                  \
+            float dist = pos[i * coord + axis] * inv_cell_size;                 \
+            AXISFN(dist, dims, index[axis], C[axis]);                           \
+        }                                                                       \
+        float w = W ? W[i] : 1.0f;                                              \
+        for (l = 0; l < NT; l++)                                                \
+            for (m = 0; m < NT; m++)                                            \
+                for (q = 0; q < NT; q++) {                                      \
+                    long o = index[0][l]*sx + index[1][m]*sy + index[2][q];     \
+                    if (W) g[o] += C[0][l]*C[1][m]*C[2][q]*w;                   \
+                    else   g[o] += C[0][l]*C[1][m]*C[2][q];                     \
+                }                                                               \
+    }
+
+void orc_tsc(const float *pos, long n, int coord, const float *W, float *g,
+             int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_SPLINE(3, tsc_axis)
+}
+
+void orc_tsc_d(const float *pos, long n, int coord, const float *W, double *g,
+               int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_SPLINE(3, tsc_axis)
+}
+
+void orc_pcs(const float *pos, long n, int coord, const float *W, float *g,
+             int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_SPLINE(4, pcs_axis)
+}
+
+void orc_pcs_d(const float *pos, long n, int coord, const float *W, double *g,
+               int dims, float box)
+{
+    int dz = (coord == 3) ? dims : 1;
+    DEPOSIT_BODY_SPLINE(4, pcs_axis)
+}
+
+/* ------------------------------------------------------------------------ */
+/* OpenMP deposit, 3D only: the reference's threaded C kernels (MAS_c.c:8-266,
+ * reached through NGPc3D..PCSWc3D, MAS_library.pyx:1305-1389): a parallel
+ * loop over particles with `#pragma omp atomic` on every tap (MAS_c.c:41,64).
+ * Used as the timed CPU baseline of the deposit.  mas: 1 NGP 2 CIC 3 TSC 4 PCS */
+/* ------------------------------------------------------------------------ */
+void orc_deposit_omp(int mas, const float *pos, long n, const float *W,
+                     float *g, int dims, float box, int threads)
+{
+    const float inv_cell_size = dims * 1.0f / box;
+    const long a = (long)dims * dims, b = dims;
+#ifdef _OPENMP
+    if (threads < 1) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(static)
+#endif
+    for (long i = 0; i < n; i++) {
+        float WW = W ? W[i] : 1.0f;
+        if (mas == 1) {
+            int idx[3];
+            for (int ax = 0; ax < 3; ax++)
+                idx[ax] = ((int)(pos[3*i+ax] * inv_cell_size + 0.5)) % dims;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+            g[idx[0]*a + idx[1]*b + idx[2]] += WW;
+        } else if (mas == 2) {
+            float C[3][2];
+            int index[3][2];
+            for (int ax = 0; ax < 3; ax++) {
+                float dist = pos[3*i+ax] * inv_cell_size;
+                C[ax][1] = dist - (int)dist;
+                C[ax][0] = 1.0f - C[ax][1];
+                index[ax][0] = ((int)dist) % dims;
+                index[ax][1] = (index[ax][0] + 1) % dims;
+            }
+            for (int l = 0; l < 2; l++)
+                for (int m = 0; m < 2; m++)
+                    for (int q = 0; q < 2; q++) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                        g[index[0][l]*a + index[1][m]*b + index[2][q]] +=
+                            C[0][l]*C[1][m]*C[2][q]*WW;
+                    }
+        } else if (mas == 3) {
+            float C[3][3];
+            int index[3][3];
+            for (int ax = 0; ax < 3; ax++)
+                tsc_axis(pos[3*i+ax] * inv_cell_size, dims, index[ax], C[ax]);
+            for (int l = 0; l < 3; l++)
+                for (int m = 0; m < 3; m++)
+                    for (int q = 0; q < 3; q++) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                        g[index[0][l]*a + index[1][m]*b + index[2][q]] +=
+                            C[0][l]*C[1][m]*C[2][q]*WW;
+                    }
+        } else {
+            float C[3][4];
+            int index[3][4];
+            for (int ax = 0; ax < 3; ax++)
+                pcs_axis(pos[3*i+ax] * inv_cell_size, dims, index[ax], C[ax]);
+            for (int l = 0; l < 4; l++)
+                for (int m = 0; m < 4; m++)
+                    for (int q = 0; q < 4; q++) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                        g[index[0][l]*a + index[1][m]*b + index[2][q]] +=
+                            C[0][l]*C[1][m]*C[2][q]*WW;
+                    }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pk mode loop (Pk_library.pyx:311-378).  dk is the unnormalised r2c output
+ * (dims, dims, dims//2+1) complex64 stored as interleaved float pairs; it is
+ * read, not modified (the reference rescales it in place, :352).  Output
+ * arrays are zero-initialised by the caller with the reference's sizes:
+ *   k1D, Pk1D, N1D            kmax_par+1         (:292-294)
+ *   Pk2D, N2D                 (kmax_par+1)*(kmax_per+1)  (:297-298)
+ *   k3D, Pk3D[.,3], Pkphase, N3D   kmax+1        (:302-305)
+ * `row0, row1` restrict the outer kxx loop to [row0, row1) so that the CPU
+ * baseline can time a bounded sample of the loop; pass 0, dims for all.    */
+/* ------------------------------------------------------------------------ */
+static double mas_correction(double x, int p)
+{
+    return (x == 0.0) ? 1.0 : pow(x / sin(x), p);   /* :83-84 */
+}
+
+void orc_pk_bin(const float *dk, int dims, int axis, int MAS_index,
+                int row0, int row1,
+                double *k1D, double *Pk1D, double *N1D,
+                double *Pk2D, double *N2D,
+                double *k3D, double *Pk3D, double *Pkphase, double *N3D)
+{
+    const int middle = dims / 2;
+    const int kmax_par = middle;
+    const int h = middle + 1;
+    const double prefact = M_PI / dims;
+    double MAS_corr[3];
+    for (int kxx = row0; kxx < row1; kxx++) {
+        int kx = (kxx > middle) ? kxx - dims : kxx;
+        MAS_corr[0] = mas_correction(prefact * kx, MAS_index);
+        for (int kyy = 0; kyy < dims; kyy++) {
+            int ky = (kyy > middle) ? kyy - dims : kyy;
+            MAS_corr[1] = mas_correction(prefact * ky, MAS_index);
+            for (int kzz = 0; kzz < middle + 1; kzz++) {
+                int kz = (kzz > middle) ? kzz - dims : kzz;
+                MAS_corr[2] = mas_correction(prefact * kz, MAS_index);
+
+                /* Hermitian half-space: kz=0 and kz=middle planes, :324-327 */
+                if (kz == 0 || (kz == middle && dims % 2 == 0)) {
+                    if (kx < 0) continue;
+                    else if (kx == 0 || (kx == middle && dims % 2 == 0)) {
+                        if (ky < 0.0) continue;
+                    }
+                }
+                double k = sqrt((double)(kx*kx + ky*ky + kz*kz));
+                int k_index = (int)k;
+                int k_par, k_per;
+                if (axis == 0)      { k_par = kx; k_per = (int)sqrt((double)(ky*ky + kz*kz)); }
+                else if (axis == 1) { k_par = ky; k_per = (int)sqrt((double)(kx*kx + kz*kz)); }
+                else                { k_par = kz; k_per = (int)sqrt((double)(kx*kx + ky*ky)); }
+                double mu = (k == 0) ? 0.0 : k_par / k;
+                double mu2 = mu * mu;
+                if (k_par < 0) k_par = -k_par;
+
+                /* float window factor times the complex64 mode, :351-352 */
+                float MAS_factor = (float)(MAS_corr[0] * MAS_corr[1] * MAS_corr[2]);
+                size_t o = (((size_t)kxx * dims + kyy) * h + kzz) * 2;
+                float re_f = dk[o] * MAS_factor, im_f = dk[o + 1] * MAS_factor;
+                double real = re_f, imag = im_f;
+                double delta2 = real * real + imag * imag;
+                double phase = atan2(real, sqrt(delta2));
+
+                if (k <= middle) {
+                    k1D[k_par] += k_par;
+                    Pk1D[k_par] += delta2;
+                    N1D[k_par] += 1.0;
+                }
+                int index_2D = (kmax_par + 1) * k_per + k_par;
+                Pk2D[index_2D] += delta2;
+                N2D[index_2D] += 1.0;
+
+                k3D[k_index] += k;
+                Pk3D[3*k_index + 0] += delta2;
+                Pk3D[3*k_index + 1] += (delta2 * (3.0 * mu2 - 1.0) / 2.0);
+                Pk3D[3*k_index + 2] += (delta2 * (35.0 * mu2 * mu2 - 30.0 * mu2 + 3.0) / 8.0);
+                Pkphase[k_index] += phase * phase;
+                N3D[k_index] += 1.0;
+            }
+        }
+    }
+}
+
+/* Same loop in float64 throughout for the precision oracle: dk is complex128
+ * and the window is applied in double.                                     */
+void orc_pk_bin_d(const double *dk, int dims, int axis, int MAS_index,
+                  double *k3D, double *Pk3D, double *N3D)
+{
+    const int middle = dims / 2;
+    const int h = middle + 1;
+    const double prefact = M_PI / dims;
+    for (int kxx = 0; kxx < dims; kxx++) {
+        int kx = (kxx > middle) ? kxx - dims : kxx;
+        double c0 = mas_correction(prefact * kx, MAS_index);
+        for (int kyy = 0; kyy < dims; kyy++) {
+            int ky = (kyy > middle) ? kyy - dims : kyy;
+            double c1 = mas_correction(prefact * ky, MAS_index);
+            for (int kzz = 0; kzz < middle + 1; kzz++) {
+                int kz = kzz;
+                double c2 = mas_correction(prefact * kz, MAS_index);
+                if (kz == 0 || (kz == middle && dims % 2 == 0)) {
+                    if (kx < 0) continue;
+                    else if (kx == 0 || (kx == middle && dims % 2 == 0)) {
+                        if (ky < 0) continue;
+                    }
+                }
+                double k = sqrt((double)(kx*kx + ky*ky + kz*kz));
+                int k_index = (int)k;
+                int k_par = (axis == 0) ? kx : (axis == 1) ? ky : kz;
+                double mu = (k == 0) ? 0.0 : k_par / k;
+                double mu2 = mu * mu;
+                double f = c0 * c1 * c2;
+                size_t o = (((size_t)kxx * dims + kyy) * h + kzz) * 2;
+                double re = dk[o] * f, im = dk[o + 1] * f;
+                double delta2 = re * re + im * im;
+                k3D[k_index] += k;
+                Pk3D[3*k_index + 0] += delta2;
+                Pk3D[3*k_index + 1] += delta2 * (3.0 * mu2 - 1.0) / 2.0;
+                Pk3D[3*k_index + 2] += delta2 * (35.0 * mu2 * mu2 - 30.0 * mu2 + 3.0) / 8.0;
+                N3D[k_index] += 1.0;
+            }
+        }
+    }
+}
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,157 @@
+// Shared declarations of libpylgpu: the context, plans and the internal
+// launchers each translation unit provides.  Device code targets sm_103a.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/pylgpu.h"
+
+namespace pyl {
+
+// ------------------------------------------------------------------ FFT plan
+// A length-n complex FFT is a sequence of Stockham stages of the given radices
+// (product = n).  tw[m] = exp(-2*pi*i*m/n), computed on the host in double.
+constexpr int kMaxStages = 24;
+struct FftDesc {
+    int n;
+    int nst;
+    int radix[kMaxStages];
+};
+
+struct FftPlan {
+    FftDesc desc;
+    float2 *d_tw = nullptr;  // n entries
+};
+
+// Mode-count tables of one (dims, axis): integer counts of independent modes
+// per bin, and the sum of |k| per 3D bin, made once and cached.  Indices
+// include the DC bin (index 0), as the reference's raw arrays do.
+struct ModeTables {
+    int dims = 0, axis = 0, kmax = 0, kmax_par = 0, kmax_per = 0;
+    std::vector<double> N3D, k3Dsum;     // kmax+1
+    std::vector<double> N1D, k1Dsum;     // kmax_par+1
+    std::vector<double> N2D;             // (kmax_par+1)*(kmax_per+1)
+    long long total = 0;
+};
+
+// Accumulators of one Pk evaluation on the device (float64 sums).
+struct PkAcc {
+    double *P3 = nullptr;     // (kmax+1)*3   sum of delta2 * L_ell(mu)
+    double *P1 = nullptr;     // kmax_par+1   sum of delta2 for k <= middle
+    double *Pph = nullptr;    // kmax+1       sum of phase^2
+    double *P2D = nullptr;    // (kmax_par+1)*(kmax_per+1)
+    float2 *dc = nullptr;     // the raw (k=0) mode, for the grid mean
+};
+
+}  // namespace pyl
+
+// Pipeline stages timed (on request) with CUDA events on the context stream.
+enum PylStage {
+    ST_H2D = 0, ST_ZERO, ST_DEPOSIT, ST_SORT, ST_FFT_Z, ST_FFT_Y, ST_FFT_X, ST_PK_X,
+    ST_D2H, ST_COUNT
+};
+
+// ------------------------------------------------------------------ context
+struct pyl_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int64_t launches = 0;
+
+    bool timing = false;
+    struct Pending { int stage; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double stage_ms[ST_COUNT] = {};
+    int64_t stage_n[ST_COUNT] = {};
+
+    struct Buf { void *p = nullptr; size_t bytes = 0; };
+    std::map<std::string, Buf> ws;                       // named workspaces
+    std::map<int, pyl::FftPlan> fft;                     // per length
+    std::map<std::pair<int, int>, pyl::ModeTables> modes;  // per (dims, axis)
+    std::map<std::pair<int, int>, float *> win;          // per (dims, mas)
+};
+
+namespace pyl {
+
+// Error helpers: record a message on the context and return a status.
+int fail(pyl_ctx *ctx, int code, const std::string &msg);
+int cuda_fail(pyl_ctx *ctx, cudaError_t e, const char *what);
+#define PYL_CUDA(ctx, call)                                                  \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) return pyl::cuda_fail((ctx), e_, #call);      \
+    } while (0)
+
+// Workspace of at least `bytes`, kept across calls under `name`.
+void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status);
+
+// Stage timing: events recorded around a stage when ctx->timing is set;
+// stage_flush() waits for them and accumulates the elapsed times.
+void stage_mark(pyl_ctx *ctx, int stage, bool begin);
+int stage_flush(pyl_ctx *ctx);
+struct StageScope {
+    pyl_ctx *ctx;
+    int stage;
+    StageScope(pyl_ctx *c, int s) : ctx(c), stage(s) { stage_mark(ctx, stage, true); }
+    ~StageScope() { stage_mark(ctx, stage, false); }
+};
+
+// Plans (ctx.cu)
+const FftPlan *fft_plan(pyl_ctx *ctx, int n, int *status);
+const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status);
+const float *window_table(pyl_ctx *ctx, int dims, int mas, int *status);
+
+// ---------------------------------------------------------------- launchers
+// deposit.cu: grid += deposit of n particles (grid extent dims^2 * dz where
+// dz = dims for coord 3 and 1 for coord 2).  All pointers are device pointers.
+int deposit(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+            float *grid, int dims, float BoxSize, int mas, int flags);
+int deposit_f64(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+                double *grid, int dims, float BoxSize, int mas);
+// grid /= d over `count` elements
+int scale_grid(pyl_ctx *ctx, float *grid, int64_t count, float s);
+int scale_grid_f64(pyl_ctx *ctx, double *grid, int64_t count, double s);
+inline int deposit_any(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+                       float *grid, int dims, float BoxSize, int mas, int flags) {
+    return deposit(ctx, pos, n, coord, W, grid, dims, BoxSize, mas, flags);
+}
+inline int deposit_any(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+                       double *grid, int dims, float BoxSize, int mas, int) {
+    return deposit_f64(ctx, pos, n, coord, W, grid, dims, BoxSize, mas);
+}
+inline int scale_any(pyl_ctx *ctx, float *g, int64_t c, double s) {
+    return scale_grid(ctx, g, c, (float)s);
+}
+inline int scale_any(pyl_ctx *ctx, double *g, int64_t c, double s) {
+    return scale_grid_f64(ctx, g, c, s);
+}
+
+// fft.cu
+// r2c along the last axis of rows (rows x n real -> rows x (n/2+1) complex)
+int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n);
+// c2r along the last axis, times `scale`
+int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n,
+                 float scale);
+// in-place c2c along axis 0 (x) or 1 (y) of an (n, n, h) complex array
+int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int axis, int dir);
+
+// pk.cu
+// x-axis FFT of the (n, n, h) half-complex array (already transformed along
+// z and y) fused with the window, |delta_k|^2, Legendre weights and binning.
+int pk_bin_x(pyl_ctx *ctx, const float2 *data, int n, int axis, int mas,
+             int what, const PkAcc &acc, int kmax, int kmax_per);
+// integer mode counts of (dims, axis) into device histograms
+int mode_counts(pyl_ctx *ctx, int dims, int axis, unsigned long long *cnt_n,
+                unsigned long long *cnt1, unsigned long long *cnt2, int kmax_per);
+
+inline int isqrt_host(long long v) { return (int)__builtin_sqrt((double)v); }
+
+}  // namespace pyl

@@ -1,0 +1,684 @@
+// C ABI of libpylgpu (include/pylgpu.h): context, plans, host/device staging
+// and the finalisation of the spectra.  The kernels live in deposit.cu,
+// fft.cu and pk.cu.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+using pyl::FftPlan;
+using pyl::ModeTables;
+
+namespace pyl {
+
+int fail(pyl_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(pyl_ctx *ctx, cudaError_t e, const char *what) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    if (ctx) ctx->err = buf;
+    return e == cudaErrorMemoryAllocation ? PYL_ERR_OOM : PYL_ERR_CUDA;
+}
+
+void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status) {
+    pyl_ctx::Buf &b = ctx->ws[name];
+    if (b.bytes >= bytes && b.p) return b.p;
+    if (b.p) {
+        // the stream may still use the old buffer
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "workspace sync"); return nullptr; }
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = bytes < 256 ? 256 : bytes;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        *status = cuda_fail(ctx, e, name);
+        return nullptr;
+    }
+    b.bytes = want;
+    return b.p;
+}
+
+void stage_mark(pyl_ctx *ctx, int stage, bool begin) {
+    if (!ctx->timing) return;
+    cudaEvent_t ev;
+    if (ctx->event_pool.empty()) {
+        if (cudaEventCreate(&ev) != cudaSuccess) return;
+    } else {
+        ev = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+    }
+    cudaEventRecord(ev, ctx->stream);
+    if (begin) {
+        ctx->pending.push_back({stage, ev, nullptr});
+    } else {
+        for (auto it = ctx->pending.rbegin(); it != ctx->pending.rend(); ++it)
+            if (it->stage == stage && it->b == nullptr) { it->b = ev; return; }
+        ctx->event_pool.push_back(ev);
+    }
+}
+
+int stage_flush(pyl_ctx *ctx) {
+    for (auto &p : ctx->pending) {
+        if (p.b) {
+            PYL_CUDA(ctx, cudaEventSynchronize(p.b));
+            float ms = 0.f;
+            PYL_CUDA(ctx, cudaEventElapsedTime(&ms, p.a, p.b));
+            ctx->stage_ms[p.stage] += ms;
+            ctx->stage_n[p.stage] += 1;
+            ctx->event_pool.push_back(p.b);
+        }
+        ctx->event_pool.push_back(p.a);
+    }
+    ctx->pending.clear();
+    return PYL_OK;
+}
+
+static void factorize(int n, FftDesc &D) {
+    D.n = n;
+    D.nst = 0;
+    int m = n;
+    while (m % 8 == 0 && D.nst < kMaxStages) { D.radix[D.nst++] = 8; m /= 8; }
+    if (m % 4 == 0) { D.radix[D.nst++] = 4; m /= 4; }
+    if (m % 2 == 0) { D.radix[D.nst++] = 2; m /= 2; }
+    for (int p : {3, 5, 7}) {
+        while (m % p == 0) { D.radix[D.nst++] = p; m /= p; }
+    }
+    for (int p = 11; m > 1 && p <= m; p += 2) {
+        while (m % p == 0) { D.radix[D.nst++] = p; m /= p; }
+    }
+    if (m > 1) D.radix[D.nst++] = m;
+}
+
+const FftPlan *fft_plan(pyl_ctx *ctx, int n, int *status) {
+    auto it = ctx->fft.find(n);
+    if (it != ctx->fft.end()) return &it->second;
+    FftPlan P;
+    factorize(n, P.desc);
+    std::vector<float2> tw(n);
+    for (int m = 0; m < n; ++m) {
+        const double a = 2.0 * M_PI * (double)m / (double)n;
+        tw[m] = make_float2((float)cos(a), (float)(-sin(a)));
+    }
+    cudaError_t e = cudaMalloc(&P.d_tw, sizeof(float2) * n);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle table"); return nullptr; }
+    e = cudaMemcpy(P.d_tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle upload"); return nullptr; }
+    return &(ctx->fft[n] = P);
+}
+
+// MAS_correction (Pk_library.pyx:83-84): 1 if x == 0 else (x / sin x)^p,
+// x = pi * k / dims with k the signed frequency of index i.
+const float *window_table(pyl_ctx *ctx, int dims, int mas, int *status) {
+    if (mas < 1 || mas > 4) mas = 0;
+    auto key = std::make_pair(dims, mas);
+    auto it = ctx->win.find(key);
+    if (it != ctx->win.end()) return it->second;
+    const int middle = dims / 2;
+    std::vector<float> w(dims);
+    const double prefact = M_PI / dims;
+    for (int i = 0; i < dims; ++i) {
+        const int k = i > middle ? i - dims : i;
+        const double x = prefact * k;
+        w[i] = (float)((x == 0.0) ? 1.0 : pow(x / sin(x), mas));
+    }
+    float *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(float) * dims);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "window table"); return nullptr; }
+    e = cudaMemcpy(d, w.data(), sizeof(float) * dims, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "window upload"); return nullptr; }
+    ctx->win[key] = d;
+    return d;
+}
+
+static void sizes(int dims, int &kmax, int &kmax_par, int &kmax_per) {
+    const long long middle = dims / 2;
+    kmax_par = (int)middle;
+    kmax_per = isqrt_host(2 * middle * middle);
+    kmax = isqrt_host(3 * middle * middle);
+}
+
+const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status) {
+    if (axis != 0 && axis != 1) axis = 2;
+    auto key = std::make_pair(dims, axis);
+    auto it = ctx->modes.find(key);
+    if (it != ctx->modes.end()) return &it->second;
+    ModeTables T;
+    T.dims = dims;
+    T.axis = axis;
+    sizes(dims, T.kmax, T.kmax_par, T.kmax_per);
+    const long long middle = dims / 2;
+    const size_t nn = (size_t)(3 * middle * middle + 1);
+    const size_t n1 = (size_t)(middle + 1);
+    const size_t n2 = (size_t)(middle + 1) * (T.kmax_per + 1);
+    int st = PYL_OK;
+    unsigned long long *d = (unsigned long long *)ws_get(
+        ctx, "mode_counts", sizeof(unsigned long long) * (nn + n1 + n2), &st);
+    if (!d) { *status = st; return nullptr; }
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * (nn + n1 + n2), ctx->stream);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count memset"); return nullptr; }
+    if ((st = mode_counts(ctx, dims, axis, d, d + nn, d + nn + n1, T.kmax_per))) {
+        *status = st;
+        return nullptr;
+    }
+    std::vector<unsigned long long> h(nn + n1 + n2);
+    e = cudaMemcpyAsync(h.data(), d, sizeof(unsigned long long) * h.size(),
+                        cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count download"); return nullptr; }
+    T.N3D.assign(T.kmax + 1, 0.0);
+    T.k3Dsum.assign(T.kmax + 1, 0.0);
+    for (size_t v = 0; v < nn; ++v) {
+        if (!h[v]) continue;
+        const int b = isqrt_host((long long)v);
+        T.N3D[b] += (double)h[v];
+        T.k3Dsum[b] += (double)h[v] * sqrt((double)v);
+        T.total += (long long)h[v];
+    }
+    T.N1D.resize(n1);
+    T.k1Dsum.resize(n1);
+    for (size_t i = 0; i < n1; ++i) {
+        T.N1D[i] = (double)h[nn + i];
+        T.k1Dsum[i] = (double)h[nn + i] * (double)i;
+    }
+    T.N2D.resize(n2);
+    for (size_t i = 0; i < n2; ++i) T.N2D[i] = (double)h[nn + n1 + i];
+    return &(ctx->modes[key] = T);
+}
+
+}  // namespace pyl
+
+using namespace pyl;
+
+// ====================================================================== ABI
+extern "C" {
+
+int pyl_ctx_create(pyl_ctx **out, int device, void *stream) {
+    if (!out) return PYL_ERR_ARG;
+    *out = nullptr;
+    pyl_ctx *ctx = new pyl_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete ctx; return PYL_ERR_CUDA; }
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete ctx; return PYL_ERR_CUDA; }
+        ctx->own_stream = true;
+    }
+    *out = ctx;
+    return PYL_OK;
+}
+
+static void release_all(pyl_ctx *ctx) {
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->ws) if (kv.second.p) cudaFree(kv.second.p);
+    ctx->ws.clear();
+    for (auto &kv : ctx->fft) cudaFree(kv.second.d_tw);
+    ctx->fft.clear();
+    for (auto &kv : ctx->win) cudaFree(kv.second);
+    ctx->win.clear();
+}
+
+int pyl_ctx_destroy(pyl_ctx *ctx) {
+    if (!ctx) return PYL_OK;
+    cudaSetDevice(ctx->device);
+    release_all(ctx);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PYL_OK;
+}
+
+int pyl_ctx_set_stream(pyl_ctx *ctx, void *stream) {
+    if (!ctx) return PYL_ERR_ARG;
+    PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+        ctx->own_stream = false;
+    } else {
+        PYL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    return PYL_OK;
+}
+
+int pyl_ctx_get_stream(const pyl_ctx *ctx, void **stream) {
+    if (!ctx || !stream) return PYL_ERR_ARG;
+    *stream = (void *)ctx->stream;
+    return PYL_OK;
+}
+
+int pyl_synchronize(pyl_ctx *ctx) {
+    if (!ctx) return PYL_ERR_ARG;
+    PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PYL_OK;
+}
+
+const char *pyl_last_error(const pyl_ctx *ctx) {
+    return ctx ? ctx->err.c_str() : "no context";
+}
+
+int pyl_ctx_workspace_bytes(const pyl_ctx *ctx, size_t *bytes) {
+    if (!ctx || !bytes) return PYL_ERR_ARG;
+    size_t s = 0;
+    for (auto &kv : ctx->ws) s += kv.second.bytes;
+    for (auto &kv : ctx->fft) s += sizeof(float2) * kv.second.desc.n;
+    *bytes = s;
+    return PYL_OK;
+}
+
+int pyl_ctx_trim(pyl_ctx *ctx) {
+    if (!ctx) return PYL_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    release_all(ctx);
+    return PYL_OK;
+}
+
+int pyl_ctx_set_timing(pyl_ctx *ctx, int on) {
+    if (!ctx) return PYL_ERR_ARG;
+    int st = stage_flush(ctx);
+    ctx->timing = on != 0;
+    return st;
+}
+
+int pyl_ctx_stage_times(pyl_ctx *ctx, double *ms, int64_t *counts, int n, int reset) {
+    if (!ctx) return PYL_ERR_ARG;
+    int st = stage_flush(ctx);
+    if (st) return st;
+    for (int i = 0; i < n && i < ST_COUNT; ++i) {
+        if (ms) ms[i] = ctx->stage_ms[i];
+        if (counts) counts[i] = ctx->stage_n[i];
+    }
+    if (reset) {
+        for (int i = 0; i < ST_COUNT; ++i) { ctx->stage_ms[i] = 0.0; ctx->stage_n[i] = 0; }
+    }
+    return ST_COUNT;
+}
+
+const char *pyl_stage_name(int stage) {
+    static const char *names[ST_COUNT] = {"h2d", "zero", "deposit", "sort", "fft_z",
+                                          "fft_y", "fft_x", "pk_x", "d2h"};
+    return (stage >= 0 && stage < ST_COUNT) ? names[stage] : "";
+}
+
+int pyl_ctx_launch_count(const pyl_ctx *ctx, int64_t *count) {
+    if (!ctx || !count) return PYL_ERR_ARG;
+    *count = ctx->launches;
+    return PYL_OK;
+}
+
+int pyl_host_alloc(void **ptr, size_t bytes) {
+    if (!ptr) return PYL_ERR_ARG;
+    cudaError_t e = cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable);
+    if (e != cudaSuccess) { *ptr = nullptr; return PYL_ERR_OOM; }
+    return PYL_OK;
+}
+
+int pyl_host_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
+    return PYL_OK;
+}
+
+int pyl_pk_sizes(int dims, int *kmax, int *kmax_par, int *kmax_per) {
+    if (dims < 2 || !kmax || !kmax_par || !kmax_per) return PYL_ERR_ARG;
+    sizes(dims, *kmax, *kmax_par, *kmax_per);
+    return PYL_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------- MA
+template <typename G>
+static int ma_impl(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+                   G *grid, int dims, float BoxSize, int mas, int renormalize_2D, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (coord != 2 && coord != 3)
+        return fail(ctx, PYL_ERR_ARG, "pos must have 2 or 3 columns");
+    if (dims < 1) return fail(ctx, PYL_ERR_ARG, "dims must be positive");
+    if (mas < PYL_MAS_NGP || mas > PYL_MAS_PCS)
+        return fail(ctx, PYL_ERR_ARG, "option not valid!!!");
+    if (n < 0 || (n > 0 && !pos) || !grid) return fail(ctx, PYL_ERR_ARG, "null array");
+    PYL_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t cells = (int64_t)dims * dims * (coord == 3 ? dims : 1);
+    const bool dev = flags & PYL_DEVICE_PTRS;
+    int st = PYL_OK;
+    const float *dpos = pos, *dW = W;
+    G *dgrid = grid;
+    if (!dev) {
+        if (n > 0) {
+            float *p = (float *)ws_get(ctx, "ma_pos", sizeof(float) * (size_t)(n * coord), &st);
+            if (!p) return st;
+            PYL_CUDA(ctx, cudaMemcpyAsync(p, pos, sizeof(float) * (size_t)(n * coord),
+                                          cudaMemcpyHostToDevice, ctx->stream));
+            dpos = p;
+        }
+        if (W && n > 0) {
+            float *w = (float *)ws_get(ctx, "ma_w", sizeof(float) * (size_t)n, &st);
+            if (!w) return st;
+            PYL_CUDA(ctx, cudaMemcpyAsync(w, W, sizeof(float) * (size_t)n,
+                                          cudaMemcpyHostToDevice, ctx->stream));
+            dW = w;
+        }
+        dgrid = (G *)ws_get(ctx, "ma_grid", sizeof(G) * (size_t)cells, &st);
+        if (!dgrid) return st;
+        PYL_CUDA(ctx, cudaMemcpyAsync(dgrid, grid, sizeof(G) * (size_t)cells,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if ((st = deposit_any(ctx, dpos, n, coord, dW, dgrid, dims, BoxSize, mas, flags))) return st;
+    if (coord == 2 && renormalize_2D && mas != PYL_MAS_NGP) {
+        // MA divides the whole 2D grid by 2, 3, 4 (MAS_library.pyx:88-110)
+        if ((st = scale_any(ctx, dgrid, cells, (double)mas))) return st;
+    }
+    if (!dev) {
+        PYL_CUDA(ctx, cudaMemcpyAsync(grid, dgrid, sizeof(G) * (size_t)cells,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+        PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return PYL_OK;
+}
+
+extern "C" {
+
+int pyl_ma(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+           float *grid, int dims, float BoxSize, int mas, int renormalize_2D, int flags) {
+    return ma_impl<float>(ctx, pos, n, coord, W, grid, dims, BoxSize, mas, renormalize_2D, flags);
+}
+
+int pyl_ma_f64(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
+               double *grid, int dims, float BoxSize, int mas, int renormalize_2D, int flags) {
+    return ma_impl<double>(ctx, pos, n, coord, W, grid, dims, BoxSize, mas, renormalize_2D,
+                           flags);
+}
+
+// --------------------------------------------------------------------- FFT
+int pyl_fft_r2c(pyl_ctx *ctx, const float *in, float *out, int dims, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (dims < 2 || !in || !out) return fail(ctx, PYL_ERR_ARG, "bad FFT arguments");
+    PYL_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int h = dims / 2 + 1;
+    const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
+    const size_t cb = sizeof(float2) * (size_t)dims * dims * h;
+    const bool dev = flags & PYL_DEVICE_PTRS;
+    int st = PYL_OK;
+    const float *din = in;
+    float2 *dout = (float2 *)out;
+    if (!dev) {
+        float *p = (float *)ws_get(ctx, "fft_real", rb, &st);
+        if (!p) return st;
+        PYL_CUDA(ctx, cudaMemcpyAsync(p, in, rb, cudaMemcpyHostToDevice, ctx->stream));
+        din = p;
+        dout = (float2 *)ws_get(ctx, "fft_cplx", cb, &st);
+        if (!dout) return st;
+    }
+    if ((st = fft_rows_r2c(ctx, din, dout, (long long)dims * dims, dims))) return st;
+    if ((st = fft_axis_c2c(ctx, dout, dims, h, 1, -1))) return st;
+    if ((st = fft_axis_c2c(ctx, dout, dims, h, 0, -1))) return st;
+    if (!dev) {
+        PYL_CUDA(ctx, cudaMemcpyAsync(out, dout, cb, cudaMemcpyDeviceToHost, ctx->stream));
+        PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return PYL_OK;
+}
+
+int pyl_fft_c2r(pyl_ctx *ctx, const float *in, float *out, int dims, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (dims < 2 || !in || !out) return fail(ctx, PYL_ERR_ARG, "bad FFT arguments");
+    PYL_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int h = dims / 2 + 1;
+    const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
+    const size_t cb = sizeof(float2) * (size_t)dims * dims * h;
+    const bool dev = flags & PYL_DEVICE_PTRS;
+    int st = PYL_OK;
+    // the input is not modified: transform a copy (as the reference copies
+    // into its aligned buffer, Pk_library.pyx:162)
+    float2 *work = (float2 *)ws_get(ctx, "fft_cplx", cb, &st);
+    if (!work) return st;
+    PYL_CUDA(ctx, cudaMemcpyAsync(work, in, cb,
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    float *dout = out;
+    if (!dev) {
+        dout = (float *)ws_get(ctx, "fft_real", rb, &st);
+        if (!dout) return st;
+    }
+    if ((st = fft_axis_c2c(ctx, work, dims, h, 0, +1))) return st;
+    if ((st = fft_axis_c2c(ctx, work, dims, h, 1, +1))) return st;
+    const double norm = 1.0 / ((double)dims * dims * dims);
+    if ((st = fft_rows_c2r(ctx, work, dout, (long long)dims * dims, dims, (float)norm))) return st;
+    if (!dev) {
+        PYL_CUDA(ctx, cudaMemcpyAsync(out, dout, rb, cudaMemcpyDeviceToHost, ctx->stream));
+        PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return PYL_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------- Pk
+namespace {
+
+struct AccLayout {
+    size_t n3, n1, nph, n2;
+    size_t bytes() const { return sizeof(double) * (n3 + n1 + nph + n2) + 64; }
+};
+
+AccLayout acc_layout(const ModeTables &T) {
+    AccLayout L;
+    L.n3 = 3 * (size_t)(T.kmax + 1);
+    L.n1 = (size_t)T.kmax_par + 1;
+    L.nph = (size_t)T.kmax + 1;
+    L.n2 = (size_t)(T.kmax_par + 1) * (T.kmax_per + 1);
+    return L;
+}
+
+PkAcc acc_view(void *base, const AccLayout &L) {
+    PkAcc a;
+    double *d = (double *)base;
+    a.P3 = d;
+    a.P1 = a.P3 + L.n3;
+    a.Pph = a.P1 + L.n1;
+    a.P2D = a.Pph + L.nph;
+    a.dc = (float2 *)(a.P2D + L.n2);
+    return a;
+}
+
+// z-r2c and y-c2c of a device grid into the half-complex workspace, then the
+// fused x pass; sums are left in acc (device).
+int pk_device(pyl_ctx *ctx, const float *dgrid, int dims, int axis, int mas, int what,
+              const ModeTables &T, void **acc_out, AccLayout &L) {
+    int st = PYL_OK;
+    const int h = dims / 2 + 1;
+    const size_t cb = sizeof(float2) * (size_t)dims * dims * h;
+    float2 *half = (float2 *)ws_get(ctx, "pk_half", cb, &st);
+    if (!half) return st;
+    L = acc_layout(T);
+    void *acc = ws_get(ctx, "pk_acc", L.bytes(), &st);
+    if (!acc) return st;
+    PYL_CUDA(ctx, cudaMemsetAsync(acc, 0, L.bytes(), ctx->stream));
+    {
+        StageScope s(ctx, ST_FFT_Z);
+        if ((st = fft_rows_r2c(ctx, dgrid, half, (long long)dims * dims, dims))) return st;
+    }
+    {
+        StageScope s(ctx, ST_FFT_Y);
+        if ((st = fft_axis_c2c(ctx, half, dims, h, 1, -1))) return st;
+    }
+    {
+        StageScope s(ctx, ST_PK_X);
+        if ((st = pk_bin_x(ctx, half, dims, axis, mas, what, acc_view(acc, L), T.kmax,
+                           T.kmax_per)))
+            return st;
+    }
+    *acc_out = acc;
+    return PYL_OK;
+}
+
+// Finalisation of class Pk (Pk_library.pyx:384-418) from the raw float64
+// sums.  inv_mean2 rescales the data sums (1 for a delta input).
+int finalize(pyl_ctx *ctx, const ModeTables &T, const std::vector<double> &raw,
+             const AccLayout &L, double BoxSize, int what, double inv_mean2,
+             bool zero_dc2d, pyl_pk_out *out) {
+    const int dims = T.dims;
+    const long long own = (dims % 2 == 1) ? 1 : 8;
+    const long long d3 = (long long)dims * dims * dims;
+    const long long expected = (d3 - own) / 2 + own;
+    if (T.total != expected) {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "WARNING: Not all modes counted: counted %lld independent modes, expected %lld",
+                 T.total, expected);
+        return fail(ctx, PYL_ERR_MODES, buf);
+    }
+    const double kF = 2.0 * M_PI / BoxSize;
+    const double kN = (dims / 2) * kF;
+    const double unit = pow(BoxSize / (double)((long long)dims * dims), 3);
+    const double *P3 = raw.data();
+    const double *P1 = P3 + L.n3;
+    const double *Pph = P1 + L.n1;
+    const double *P2 = Pph + L.nph;
+    for (int b = 1; b <= T.kmax; ++b) {
+        const double N = T.N3D[b];
+        if (out->k3D) out->k3D[b - 1] = (T.k3Dsum[b] / N) * kF;
+        if (out->Nmodes3D) out->Nmodes3D[b - 1] = N;
+        if (out->Pk) {
+            out->Pk[3 * (b - 1) + 0] = (P3[3 * b + 0] * inv_mean2 / N) * unit;
+            out->Pk[3 * (b - 1) + 1] = (P3[3 * b + 1] * inv_mean2 * 5.0 / N) * unit;
+            out->Pk[3 * (b - 1) + 2] = (P3[3 * b + 2] * inv_mean2 * 9.0 / N) * unit;
+        }
+        if ((what & PYL_PK_PHASE) && out->Pkphase) out->Pkphase[b - 1] = (Pph[b] / N) * unit;
+    }
+    if (what & PYL_PK_1D) {
+        for (int i = 1; i <= T.kmax_par; ++i) {
+            const double N = T.N1D[i];
+            double pk = P1[i] * inv_mean2 * unit;
+            const double k1 = (T.k1Dsum[i] / N) * kF;
+            const double kmaxper = sqrt(kN * kN - k1 * k1);
+            pk = pk * (M_PI * kmaxper * kmaxper / N) / ((2.0 * M_PI) * (2.0 * M_PI));
+            if (out->k1D) out->k1D[i - 1] = k1;
+            if (out->Pk1D) out->Pk1D[i - 1] = pk;
+            if (out->Nmodes1D) out->Nmodes1D[i - 1] = N;
+        }
+    }
+    if (what & PYL_PK_2D) {
+        const int np = T.kmax_par + 1, nq = T.kmax_per + 1;
+        for (int q = 0; q < nq; ++q)
+            for (int p = 0; p < np; ++p) {
+                const size_t i = (size_t)np * q + p;
+                if (out->kpar) out->kpar[i] = 0.5 * (p + p + 1) * kF;
+                if (out->kper) out->kper[i] = 0.5 * (q + q + 1) * kF;
+                double s = P2[i] * inv_mean2;
+                if (zero_dc2d && i == 0) s = 0.0;
+                if (out->Pk2D) out->Pk2D[i] = s * unit / T.N2D[i];
+                if (out->Nmodes2D) out->Nmodes2D[i] = T.N2D[i];
+            }
+    }
+    return PYL_OK;
+}
+
+int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double> &raw,
+                 float2 *dc) {
+    raw.resize(L.n3 + L.n1 + L.nph + L.n2 + 8);
+    {
+        StageScope s(ctx, ST_D2H);
+        PYL_CUDA(ctx, cudaMemcpyAsync(raw.data(), acc, L.bytes() - 64 + sizeof(float2),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    memcpy(dc, (const char *)raw.data() + sizeof(double) * (L.n3 + L.n1 + L.nph + L.n2),
+           sizeof(float2));
+    return PYL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pyl_pk(pyl_ctx *ctx, const float *delta, int dims, double BoxSize, int axis, int mas,
+           int what, pyl_pk_out *out, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (dims < 2 || !delta || !out) return fail(ctx, PYL_ERR_ARG, "bad Pk arguments");
+    PYL_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = PYL_OK;
+    const ModeTables *T = mode_tables(ctx, dims, axis, &st);
+    if (!T) return st;
+    const float *dgrid = delta;
+    if (!(flags & PYL_DEVICE_PTRS)) {
+        const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
+        float *p = (float *)ws_get(ctx, "pk_grid", rb, &st);
+        if (!p) return st;
+        PYL_CUDA(ctx, cudaMemcpyAsync(p, delta, rb, cudaMemcpyHostToDevice, ctx->stream));
+        dgrid = p;
+    }
+    void *acc = nullptr;
+    AccLayout L;
+    if ((st = pk_device(ctx, dgrid, dims, axis, mas, what, *T, &acc, L))) return st;
+    std::vector<double> raw;
+    float2 dc;
+    if ((st = download_raw(ctx, acc, L, raw, &dc))) return st;
+    return finalize(ctx, *T, raw, L, BoxSize, what, 1.0, false, out);
+}
+
+int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n, const float *W, int dims,
+                     float BoxSize, int mas_deposit, int axis, int mas_window, int what,
+                     pyl_pk_out *out, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (dims < 2 || !out || n <= 0 || !pos) return fail(ctx, PYL_ERR_ARG, "bad arguments");
+    if (mas_deposit < PYL_MAS_NGP || mas_deposit > PYL_MAS_PCS)
+        return fail(ctx, PYL_ERR_ARG, "option not valid!!!");
+    PYL_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = PYL_OK;
+    const ModeTables *T = mode_tables(ctx, dims, axis, &st);
+    if (!T) return st;
+    const float *dpos = pos, *dW = W;
+    if (!(flags & PYL_DEVICE_PTRS)) {
+        StageScope s(ctx, ST_H2D);
+        float *p = (float *)ws_get(ctx, "ma_pos", sizeof(float) * (size_t)(3 * n), &st);
+        if (!p) return st;
+        PYL_CUDA(ctx, cudaMemcpyAsync(p, pos, sizeof(float) * (size_t)(3 * n),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        dpos = p;
+        if (W) {
+            float *w = (float *)ws_get(ctx, "ma_w", sizeof(float) * (size_t)n, &st);
+            if (!w) return st;
+            PYL_CUDA(ctx, cudaMemcpyAsync(w, W, sizeof(float) * (size_t)n,
+                                          cudaMemcpyHostToDevice, ctx->stream));
+            dW = w;
+        }
+    }
+    const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
+    float *grid = (float *)ws_get(ctx, "pk_grid", rb, &st);
+    if (!grid) return st;
+    {
+        StageScope s(ctx, ST_ZERO);
+        PYL_CUDA(ctx, cudaMemsetAsync(grid, 0, rb, ctx->stream));
+    }
+    {
+        StageScope s(ctx, ST_DEPOSIT);
+        if ((st = deposit(ctx, dpos, n, 3, dW, grid, dims, BoxSize, mas_deposit, flags)))
+            return st;
+    }
+    void *acc = nullptr;
+    AccLayout L;
+    if ((st = pk_device(ctx, grid, dims, axis, mas_window, what, *T, &acc, L))) return st;
+    std::vector<double> raw;
+    float2 dc;
+    if ((st = download_raw(ctx, acc, L, raw, &dc))) return st;
+    // mean of the grid = DC mode / dims^3; P(delta) = P(rho) / mean^2
+    const double mean = (double)dc.x / ((double)dims * dims * dims);
+    if (!(mean > 0.0) && !(mean < 0.0))
+        return fail(ctx, PYL_ERR_ARG, "grid mean is zero: cannot form the overdensity");
+    return finalize(ctx, *T, raw, L, BoxSize, what, 1.0 / (mean * mean), true, out);
+}
+
+}  // extern "C"

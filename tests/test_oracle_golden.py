@@ -1,0 +1,113 @@
+"""Pin the CPU oracle (oracle/) to the golden vectors made by the reference.
+
+The golden vectors (tests/golden/*.npz) were produced by the reference's own
+compiled MAS_library / Pk_library (tests/golden/make_golden.py).  The oracle
+must reproduce them: mode counts and k-bins exactly, grids to float32
+rounding (the reference was built with -ffast-math, which contracts some
+multiply-adds), spectra to float64 rounding.
+"""
+import numpy as np
+import pytest
+
+BOX = 1000.0
+KEYS = ("k3D", "Pk", "Nmodes3D", "k1D", "Pk1D", "Nmodes1D", "kpar", "kper",
+        "Pk2D", "Nmodes2D", "Pkphase")
+
+
+@pytest.mark.parametrize("dims", [16, 17])
+@pytest.mark.parametrize("coord", [3, 2])
+@pytest.mark.parametrize("MAS", ["NGP", "CIC", "TSC", "PCS"])
+@pytest.mark.parametrize("wt", [0, 1])
+def test_ma_matches_reference(golden, oracle, dims, coord, MAS, wt):
+    g = golden["ma"]
+    tag = "d%d_c%d" % (dims, coord)
+    pos, W = g["pos_" + tag], g["W_" + tag]
+    ref = g["grid_%s_%s_w%d" % (tag, MAS, wt)]
+    grid = np.zeros((dims,) * coord, np.float32)
+    oracle.MA(pos, grid, BOX, MAS, W=W if wt else None)
+    scale = max(1.0, float(np.abs(ref).max()))
+    assert np.abs(grid - ref).max() <= 2e-6 * scale * (4 if coord == 2 else 1)
+    # mass conservation, as library/tests/test.py asserts
+    mass = float(W.astype(np.float64).sum()) if wt else float(len(pos))
+    assert abs(grid.sum(dtype=np.float64) / mass - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("dims", [16, 17, 24])
+@pytest.mark.parametrize("MAS", ["NGP", "CIC", "TSC", "PCS", "None"])
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_pk_matches_reference(golden, oracle, dims, MAS, axis):
+    g = golden["pk"]
+    delta = g["delta_d%d" % dims]
+    r = oracle.Pk(delta, BOX, axis=axis, MAS=MAS, threads=1)
+    for k in KEYS:
+        ref = g["%s_d%d_%s_a%d" % (k, dims, MAS, axis)]
+        got = np.asarray(getattr(r, k))
+        assert got.shape == ref.shape, k
+        if k.startswith("Nmodes"):
+            assert np.array_equal(got, ref), k
+        elif k == "Pk":
+            # multipoles cross zero: compare against |P0| of the bin
+            err = np.abs(got - ref).max(axis=1) / np.abs(ref[:, 0])
+            assert err.max() < 1e-12, (k, err.max())
+        else:
+            fin = np.isfinite(ref)
+            assert np.array_equal(fin, np.isfinite(got)), k
+            scale = np.abs(ref[fin]).max() if fin.any() else 1.0
+            assert np.abs(got[fin] - ref[fin]).max(initial=0.0) <= 1e-12 * scale, k
+
+
+@pytest.mark.parametrize("dims", [8, 9, 63, 64, 128])
+def test_mode_counts_match_reference(golden, oracle, dims):
+    g = golden["nmodes"]
+    z = np.zeros((dims,) * 3, np.float32)
+    r = oracle.Pk(z, BOX, axis=2, MAS="CIC")
+    assert np.array_equal(r.Nmodes3D, g["Nmodes3D_d%d" % dims])
+    assert np.array_equal(r.Nmodes1D, g["Nmodes1D_d%d" % dims])
+    assert np.array_equal(r.Nmodes2D, g["Nmodes2D_d%d" % dims])
+    np.testing.assert_allclose(r.k3D, g["k3D_d%d" % dims], rtol=1e-13)
+    assert int(r.Nmodes3D.sum()) + 1 == oracle.expected_modes(dims)
+
+
+def test_pipeline_matches_reference(golden, oracle):
+    g = golden["pipeline"]
+    dims = g["delta"].shape[0]
+    delta = np.zeros((dims,) * 3, np.float32)
+    oracle.MA(g["pos"], delta, BOX, "CIC")
+    delta /= np.mean(delta, dtype=np.float64)
+    delta -= 1.0
+    assert np.abs(delta - g["delta"]).max() < 1e-5
+    r = oracle.Pk(delta, BOX, axis=0, MAS="CIC")
+    p0 = np.abs(g["Pk"][:, 0])
+    assert np.all(np.abs(r.Pk - g["Pk"]).max(axis=1) / p0 < 1e-5)
+    assert np.array_equal(r.Nmodes3D, g["Nmodes3D"])
+
+
+def test_fft_conventions(oracle):
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((12, 12, 12)).astype(np.float32)
+    f = oracle.FFT3Dr_f(a)
+    assert f.dtype == np.complex64 and f.shape == (12, 12, 7)
+    np.testing.assert_allclose(f, np.fft.rfftn(a.astype(np.float64)), rtol=1e-4, atol=1e-4)
+    back = oracle.IFFT3Dr_f(f)
+    np.testing.assert_allclose(back, a, atol=1e-5)
+
+
+def test_f64_oracle_close_to_f32(golden, oracle):
+    g = golden["pk"]
+    delta = g["delta_d24"]
+    r32 = oracle.Pk(delta, BOX, axis=2, MAS="CIC")
+    r64 = oracle.Pk_f64(delta.astype(np.float64), BOX, axis=2, MAS="CIC")
+    p0 = np.abs(r64.Pk[:, 0])
+    assert np.max(np.abs(r32.Pk - r64.Pk).max(axis=1) / p0) < 1e-5
+    assert np.array_equal(r32.Nmodes3D, r64.Nmodes3D)
+
+
+def test_omp_deposit_matches_serial(oracle):
+    rng = np.random.default_rng(9)
+    pos = rng.random((20000, 3), dtype=np.float32) * np.float32(BOX)
+    for MAS in ("NGP", "CIC", "TSC", "PCS"):
+        a = np.zeros((20,) * 3, np.float32)
+        b = np.zeros_like(a)
+        oracle.MA(pos, a, BOX, MAS)
+        oracle.deposit_omp(MAS, pos, b, BOX, threads=2)
+        assert np.abs(a - b).max() < 1e-5
