@@ -19,7 +19,10 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 SO = os.path.join(PKG, "libpylgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
+# -ffp-contract=off: the host-side finalisation evaluates the reference's
+# float64 formulas operation by operation (gcc contracts a*b-c into an FMA by
+# default on aarch64, which changes e.g. sqrt(kN^2 - k^2) at kN == k).
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
 

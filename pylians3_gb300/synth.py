@@ -58,8 +58,8 @@ def zeldovich(dims, BoxSize, sigma=3.0, seed=0, rsd=0.5, device="cuda"):
         psi.append(PKL.IFFT3Dr_f(comp.to(torch.complex64).contiguous(), 1))
         del comp
     del dk, k2
-    rms = torch.sqrt(sum(float(p.double().pow(2).mean()) for p in psi) / 3.0)
-    scale = float(sigma) / float(rms)
+    rms = math.sqrt(sum(float(p.double().pow(2).mean()) for p in psi) / 3.0)
+    scale = float(sigma) / rms
     cell = BoxSize / dims
     lat = (torch.arange(dims, device=device, dtype=torch.float32) + 0.5) * cell
     pos = torch.empty((dims ** 3, 3), device=device, dtype=torch.float32)

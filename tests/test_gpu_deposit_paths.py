@@ -1,0 +1,95 @@
+"""Both deposit paths (unsorted global atomics and tile-sorted shared memory),
+forced through the C ABI flags, against the oracle on uniform, clustered and
+edge-case inputs.  Grids agree to float32 rounding of a different summation
+order: |diff| <= 1e-5 * max(1, |value|)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BOX = 1000.0
+
+
+@pytest.fixture(scope="module")
+def native():
+    import torch
+    assert torch.cuda.is_available()
+    from pylians3_gb300 import build_native, _native
+    build_native.build()
+    return _native
+
+
+def run_ma(native, pos, dims, MAS, W=None, flags=0, grid=None):
+    ctx = native.context(0)
+    g = np.zeros((dims,) * 3, np.float32) if grid is None else grid
+    p = np.ascontiguousarray(pos, np.float32)
+    w = None if W is None else np.ascontiguousarray(W, np.float32)
+    ctx.check(ctx.lib.pyl_ma(ctx.ptr, ctypes.c_void_p(p.ctypes.data), len(p), 3,
+                             None if w is None else ctypes.c_void_p(w.ctypes.data),
+                             ctypes.c_void_p(g.ctypes.data), dims, ctypes.c_float(BOX),
+                             native.MAS_CODE[MAS], 0, flags))
+    return g
+
+
+def inputs(kind, n, rng):
+    if kind == "uniform":
+        return rng.random((n, 3), dtype=np.float32) * np.float32(BOX)
+    if kind == "clustered":
+        c = rng.random((20, 3)) * BOX
+        p = c[rng.integers(0, 20, n)] + rng.standard_normal((n, 3)) * 8.0
+        return np.mod(p, BOX).astype(np.float32)
+    # edges: exact cell boundaries, 0 and BoxSize and the last float below it
+    vals = np.array([0.0, BOX / 64, BOX / 2, BOX - BOX / 64, BOX,
+                     np.nextafter(np.float32(BOX), np.float32(0))], np.float32)
+    e = np.stack(np.meshgrid(vals, vals, vals, indexing="ij"), -1).reshape(-1, 3)
+    return np.concatenate([e, rng.random((n, 3), dtype=np.float32) * np.float32(BOX)])
+
+
+@pytest.mark.parametrize("dims", [32, 48, 50, 64, 128])
+@pytest.mark.parametrize("MAS", ["NGP", "CIC", "TSC", "PCS"])
+@pytest.mark.parametrize("kind", ["uniform", "clustered", "edges"])
+def test_paths_match_oracle(native, oracle, dims, MAS, kind):
+    rng = np.random.default_rng(dims * 7 + len(kind))
+    pos = inputs(kind, 200000, rng)
+    W = rng.lognormal(0, 0.5, len(pos)).astype(np.float32)
+    for w in (None, W):
+        ref = np.zeros((dims,) * 3, np.float32)
+        oracle.MA(pos, ref, BOX, MAS, W=w)
+        tol = 1e-5 * max(1.0, float(np.abs(ref).max()))
+        for flags in (native.PYL_DEPOSIT_SORTED, native.PYL_DEPOSIT_ATOMIC):
+            g = run_ma(native, pos, dims, MAS, w, flags)
+            assert float(np.abs(g - ref).max()) <= tol, (flags, w is None)
+
+
+def test_sorted_accumulates(native, oracle):
+    rng = np.random.default_rng(1)
+    pos = rng.random((300000, 3), dtype=np.float32) * np.float32(BOX)
+    base = rng.random((64,) * 3, dtype=np.float32)
+    g = run_ma(native, pos, 64, "TSC", flags=native.PYL_DEPOSIT_SORTED, grid=base.copy())
+    ref = base.copy()
+    oracle.MA(pos, ref, BOX, "TSC")
+    assert float(np.abs(g - ref).max()) <= 1e-5 * float(np.abs(ref).max())
+
+
+def test_sorted_unaligned_device_grid(native, oracle):
+    """A grid that is a view at a 4-byte offset takes the scalar flush."""
+    import torch
+    rng = np.random.default_rng(2)
+    pos = rng.random((300000, 3), dtype=np.float32) * np.float32(BOX)
+    dims = 64
+    buf = torch.zeros(dims ** 3 + 1, device="cuda")
+    view = buf[1:]
+    tp = torch.from_numpy(pos).cuda()
+    ctx = native.context(0)
+    ctx.check(ctx.lib.pyl_ma(ctx.ptr, ctypes.c_void_p(tp.data_ptr()), len(pos), 3, None,
+                             ctypes.c_void_p(view.data_ptr()), dims, ctypes.c_float(BOX),
+                             native.MAS_CODE["CIC"], 0,
+                             native.PYL_DEVICE_PTRS | native.PYL_DEPOSIT_SORTED))
+    ctx.synchronize()
+    ref = np.zeros((dims,) * 3, np.float32)
+    oracle.MA(pos, ref, BOX, "CIC")
+    assert float(buf[0].item()) == 0.0
+    got = view.cpu().numpy().reshape((dims,) * 3)
+    assert float(np.abs(got - ref).max()) <= 1e-5 * float(ref.max())
