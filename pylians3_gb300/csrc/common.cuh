@@ -134,20 +134,39 @@ inline int scale_any(pyl_ctx *ctx, double *g, int64_t c, double s) {
     return scale_grid_f64(ctx, g, c, s);
 }
 
-// fft.cu
-// r2c along the last axis of rows (rows x n real -> rows x (n/2+1) complex)
-int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n);
-// c2r along the last axis, times `scale`
-int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n,
+// fft.cu (power-of-two lengths go to fft_pow2.cu)
+// r2c along the last axis of rows (rows x n real -> rows x (n/2+1) complex,
+// output row stride ostride >= n/2+1; padding needs a power-of-two n)
+int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride);
+// c2r along the last axis, times `scale` (input row stride istride)
+int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n, int istride,
                  float scale);
-// in-place c2c along axis 0 (x) or 1 (y) of an (n, n, h) complex array
-int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int axis, int dir);
+// in-place c2c along axis 0 (x) or 1 (y) of an (n, n, h) complex array whose
+// rows have stride rs >= h
+int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int dir);
+
+// fft_pow2.cu
+bool pow2_supported(int n);
+int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
+                  const float2 *tw);
+int pow2_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n, int istride,
+                  const float2 *tw, float scale);
+int pow2_cols(pyl_ctx *ctx, float2 *data, int n, int ncol, int64_t estride, int64_t ostride,
+              int nouter, int dir, const float2 *tw);
+int pow2_pk_x(pyl_ctx *ctx, const float2 *data, int n, int rs, int axis, const float2 *tw,
+              const float *win, int kmax, const PkAcc &acc, int what);
 
 // pk.cu
 // x-axis FFT of the (n, n, h) half-complex array (already transformed along
 // z and y) fused with the window, |delta_k|^2, Legendre weights and binning.
-int pk_bin_x(pyl_ctx *ctx, const float2 *data, int n, int axis, int mas,
+int pk_bin_x(pyl_ctx *ctx, const float2 *data, int n, int rs, int axis, int mas,
              int what, const PkAcc &acc, int kmax, int kmax_per);
+// padded row stride of the internal half-complex grid (64-byte aligned rows
+// on the power-of-two path)
+inline int half_stride(int n) {
+    const int h = n / 2 + 1;
+    return (n >= 16 && (n & (n - 1)) == 0) ? (h + 7) / 8 * 8 : h;
+}
 // integer mode counts of (dims, axis) into device histograms
 int mode_counts(pyl_ctx *ctx, int dims, int axis, unsigned long long *cnt_n,
                 unsigned long long *cnt1, unsigned long long *cnt2, int kmax_per);

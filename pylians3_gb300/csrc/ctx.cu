@@ -421,9 +421,9 @@ int pyl_fft_r2c(pyl_ctx *ctx, const float *in, float *out, int dims, int flags) 
         dout = (float2 *)ws_get(ctx, "fft_cplx", cb, &st);
         if (!dout) return st;
     }
-    if ((st = fft_rows_r2c(ctx, din, dout, (long long)dims * dims, dims))) return st;
-    if ((st = fft_axis_c2c(ctx, dout, dims, h, 1, -1))) return st;
-    if ((st = fft_axis_c2c(ctx, dout, dims, h, 0, -1))) return st;
+    if ((st = fft_rows_r2c(ctx, din, dout, (long long)dims * dims, dims, h))) return st;
+    if ((st = fft_axis_c2c(ctx, dout, dims, h, h, 1, -1))) return st;
+    if ((st = fft_axis_c2c(ctx, dout, dims, h, h, 0, -1))) return st;
     if (!dev) {
         PYL_CUDA(ctx, cudaMemcpyAsync(out, dout, cb, cudaMemcpyDeviceToHost, ctx->stream));
         PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -452,10 +452,11 @@ int pyl_fft_c2r(pyl_ctx *ctx, const float *in, float *out, int dims, int flags) 
         dout = (float *)ws_get(ctx, "fft_real", rb, &st);
         if (!dout) return st;
     }
-    if ((st = fft_axis_c2c(ctx, work, dims, h, 0, +1))) return st;
-    if ((st = fft_axis_c2c(ctx, work, dims, h, 1, +1))) return st;
+    if ((st = fft_axis_c2c(ctx, work, dims, h, h, 0, +1))) return st;
+    if ((st = fft_axis_c2c(ctx, work, dims, h, h, 1, +1))) return st;
     const double norm = 1.0 / ((double)dims * dims * dims);
-    if ((st = fft_rows_c2r(ctx, work, dout, (long long)dims * dims, dims, (float)norm))) return st;
+    if ((st = fft_rows_c2r(ctx, work, dout, (long long)dims * dims, dims, h, (float)norm)))
+        return st;
     if (!dev) {
         PYL_CUDA(ctx, cudaMemcpyAsync(out, dout, rb, cudaMemcpyDeviceToHost, ctx->stream));
         PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -499,7 +500,8 @@ int pk_device(pyl_ctx *ctx, const float *dgrid, int dims, int axis, int mas, int
               const ModeTables &T, void **acc_out, AccLayout &L) {
     int st = PYL_OK;
     const int h = dims / 2 + 1;
-    const size_t cb = sizeof(float2) * (size_t)dims * dims * h;
+    const int rs = half_stride(dims);   // padded rows: 64-byte aligned column blocks
+    const size_t cb = sizeof(float2) * (size_t)dims * dims * rs;
     float2 *half = (float2 *)ws_get(ctx, "pk_half", cb, &st);
     if (!half) return st;
     L = acc_layout(T);
@@ -508,15 +510,15 @@ int pk_device(pyl_ctx *ctx, const float *dgrid, int dims, int axis, int mas, int
     PYL_CUDA(ctx, cudaMemsetAsync(acc, 0, L.bytes(), ctx->stream));
     {
         StageScope s(ctx, ST_FFT_Z);
-        if ((st = fft_rows_r2c(ctx, dgrid, half, (long long)dims * dims, dims))) return st;
+        if ((st = fft_rows_r2c(ctx, dgrid, half, (long long)dims * dims, dims, rs))) return st;
     }
     {
         StageScope s(ctx, ST_FFT_Y);
-        if ((st = fft_axis_c2c(ctx, half, dims, h, 1, -1))) return st;
+        if ((st = fft_axis_c2c(ctx, half, dims, h, rs, 1, -1))) return st;
     }
     {
         StageScope s(ctx, ST_PK_X);
-        if ((st = pk_bin_x(ctx, half, dims, axis, mas, what, acc_view(acc, L), T.kmax,
+        if ((st = pk_bin_x(ctx, half, dims, rs, axis, mas, what, acc_view(acc, L), T.kmax,
                            T.kmax_per)))
             return st;
     }

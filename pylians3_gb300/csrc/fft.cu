@@ -125,18 +125,21 @@ int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
 
 }  // namespace
 
-int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n) {
+int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n,
+                 int ostride) {
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
+    if (pow2_supported(n)) return pow2_rows_r2c(ctx, in, out, rows, n, ostride, P->d_tw);
+    if (ostride != n / 2 + 1) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     int pairs = (int)(kLineBudget / (sizeof(float2) * (size_t)n));
     if (pairs < 1) pairs = 1;
-    const long long npairs = (rows + 1) / 2;
+    const int64_t npairs = (rows + 1) / 2;
     if (pairs > npairs) pairs = (int)npairs;
     const size_t smem = sizeof(float2) * ((size_t)n + 2 * (size_t)pairs * n);
     if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "FFT length too large");
     if ((st = set_smem(ctx, k_rows_r2c<-1>, smem))) return st;
-    const long long grid = (npairs + pairs - 1) / pairs;
+    const int64_t grid = (npairs + pairs - 1) / pairs;
     k_rows_r2c<-1><<<(unsigned)grid, kThreads, smem, ctx->stream>>>(in, out, rows, P->desc,
                                                                   P->d_tw, pairs);
     ctx->launches++;
@@ -145,18 +148,20 @@ int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n
 }
 
 int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n,
-                 float scale) {
+                 int istride, float scale) {
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
+    if (pow2_supported(n)) return pow2_rows_c2r(ctx, in, out, rows, n, istride, P->d_tw, scale);
+    if (istride != n / 2 + 1) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     int pairs = (int)(kLineBudget / (sizeof(float2) * (size_t)n));
     if (pairs < 1) pairs = 1;
-    const long long npairs = (rows + 1) / 2;
+    const int64_t npairs = (rows + 1) / 2;
     if (pairs > npairs) pairs = (int)npairs;
     const size_t smem = sizeof(float2) * ((size_t)n + 2 * (size_t)pairs * n);
     if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "FFT length too large");
     if ((st = set_smem(ctx, k_rows_c2r, smem))) return st;
-    const long long grid = (npairs + pairs - 1) / pairs;
+    const int64_t grid = (npairs + pairs - 1) / pairs;
     k_rows_c2r<<<(unsigned)grid, kThreads, smem, ctx->stream>>>(in, out, rows, P->desc,
                                                               P->d_tw, pairs, scale);
     ctx->launches++;
@@ -164,10 +169,16 @@ int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n
     return PYL_OK;
 }
 
-int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int axis, int dir) {
+int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int dir) {
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
+    if (pow2_supported(n)) {
+        const int64_t plane = (int64_t)n * rs;
+        return axis == 1 ? pow2_cols(ctx, data, n, h, rs, plane, n, dir, P->d_tw)
+                         : pow2_cols(ctx, data, n, h, plane, rs, n, dir, P->d_tw);
+    }
+    if (rs != h) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     // largest power of two <= 16 whose B lines fit the line budget
     int B = 16;
     while (B > 1 && sizeof(float2) * (size_t)B * (n + 1) > kLineBudget) B >>= 1;

@@ -1,0 +1,331 @@
+// Power-of-two fast path of the 3D FFT passes and of the fused power-spectrum
+// pass (the generic mixed-radix kernels in fft.cu / pk.cu handle every other
+// length).  See fft_pow2.cuh for the register-resident FFT.
+//
+//   rows r2c / c2r : a CTA transforms L row pairs (a + i b) of length N;
+//                    loads and stores are contiguous runs along z.
+//   columns c2c    : a CTA owns C consecutive columns (kz) of one outer
+//                    index and transforms them along y or x; thread (c, t)
+//                    loads x[t + s*P] of column c directly from global memory
+//                    (C*8 contiguous bytes per element row) and stores its
+//                    natural-order result the same way.
+//   pk_x           : the x-column transform fused with the window, |delta|^2,
+//                    Legendre weights and the integer-|k| binning, straight
+//                    from registers; persistent CTAs, float32 shared
+//                    histograms folded into float64 shared sums every few
+//                    items, one float64 atomic per bin and CTA at the end.
+#include "fft_pow2.cuh"
+#include "pk_common.cuh"
+
+namespace pyl {
+
+namespace {
+
+template <int N>
+struct RowsCfg {
+    static constexpr int P = N / 8;
+    static constexpr int L = P >= 256 ? 1 : 256 / P;   // row pairs per CTA
+    static constexpr int THREADS = L * P;
+};
+
+template <int N>
+struct ColsCfg {
+    static constexpr int P = N / 8;
+    static constexpr int C = P >= 512 ? 1 : (512 / P > 8 ? 8 : 512 / P);
+    static constexpr int THREADS = C * P;
+};
+
+template <int N>
+__global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
+k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t rows, int ostride,
+              const float2 *__restrict__ g_tw) {
+    using CF = RowsCfg<N>;
+    constexpr int P = CF::P, LINE = Pow2<N>::LINE, H = N / 2 + 1;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    const int l = threadIdx.x / P, t = threadIdx.x % P;
+    float2 *line = sm + N + l * LINE;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
+    float2 v[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const float a = ra < rows ? __ldcs(in + ra * N + t + s * P) : 0.f;
+        const float b = rb < rows ? __ldcs(in + rb * N + t + s * P) : 0.f;
+        v[s] = make_float2(a, b);
+    }
+    __syncthreads();
+    fft_line<N, -1>(v, t, line, tw);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) line[pad8(t + u * P)] = v[u];
+    __syncthreads();
+    for (int k = t; k < H; k += P) {
+        const float2 Z = line[pad8(k)];
+        const float2 Zm = line[pad8((N - k) & (N - 1))];
+        if (ra < rows)
+            out[ra * ostride + k] = make_float2(0.5f * (Z.x + Zm.x), 0.5f * (Z.y - Zm.y));
+        if (rb < rows)
+            out[rb * ostride + k] = make_float2(0.5f * (Z.y + Zm.y), -0.5f * (Z.x - Zm.x));
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
+k_rows_c2r_p2(const float2 *__restrict__ in, float *__restrict__ out, int64_t rows, int istride,
+              const float2 *__restrict__ g_tw, float scale) {
+    using CF = RowsCfg<N>;
+    constexpr int P = CF::P, LINE = Pow2<N>::LINE, H = N / 2 + 1;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    const int l = threadIdx.x / P, t = threadIdx.x % P;
+    float2 *line = sm + N + l * LINE;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
+    float2 v[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int k = t + s * P;
+        const bool lower = k < H;
+        const int kk = lower ? k : N - k;
+        float2 A = ra < rows ? in[ra * istride + kk] : make_float2(0.f, 0.f);
+        float2 B = rb < rows ? in[rb * istride + kk] : make_float2(0.f, 0.f);
+        if (kk == 0 || 2 * kk == N) { A.y = 0.f; B.y = 0.f; }
+        if (!lower) { A.y = -A.y; B.y = -B.y; }
+        v[s] = make_float2(A.x - B.y, A.y + B.x);
+    }
+    __syncthreads();
+    fft_line<N, +1>(v, t, line, tw);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        if (ra < rows) out[ra * N + t + u * P] = v[u].x * scale;
+        if (rb < rows) out[rb * N + t + u * P] = v[u].y * scale;
+    }
+}
+
+// In-place c2c along one axis.  Column (outer, kz0 + c): element e at
+// data[outer * ostride + (kz0 + c) + e * estride]; columns >= ncol are idle.
+template <int N, int DIR>
+__global__ void __launch_bounds__(ColsCfg<N>::THREADS, 1)
+k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
+          const float2 *__restrict__ g_tw) {
+    using CF = ColsCfg<N>;
+    constexpr int P = CF::P, C = CF::C, LINE = Pow2<N>::LINE;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    float2 *line = sm + N + c * LINE;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    const int col = blockIdx.x * C + c;
+    const bool valid = col < ncol;
+    float2 *base = data + (int64_t)blockIdx.y * ostride + col;
+    float2 v[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+        v[s] = valid ? base[(int64_t)(t + s * P) * estride] : make_float2(0.f, 0.f);
+    __syncthreads();
+    fft_line<N, DIR>(v, t, line, tw);
+    if (valid) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) base[(int64_t)(t + u * P) * estride] = v[u];
+    }
+}
+
+// Fused x transform + binning over items (kyy, kz block), persistent CTAs.
+template <int N, int WHAT>
+__global__ void __launch_bounds__(ColsCfg<N>::THREADS, 1)
+k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restrict__ g_tw,
+          const float *__restrict__ g_win, int axis, int kmax, PkAcc acc, int nitems,
+          int fold_every) {
+    using CF = ColsCfg<N>;
+    constexpr int P = CF::P, C = CF::C, LINE = Pow2<N>::LINE;
+    constexpr int MID = N / 2;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    float2 *line = sm + N + c * LINE;
+    float *win = reinterpret_cast<float *>(sm + N + C * LINE);
+    BinHist H;
+    H.setup(win + N, kmax, MID, WHAT);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) { tw[i] = g_tw[i]; win[i] = g_win[i]; }
+    H.zero_all();
+    __syncthreads();
+    const int nzb = (h + C - 1) / C;
+    int since_fold = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int kyy = it / nzb;
+        const int kz = (it % nzb) * C + c;
+        const bool valid = kz < h;
+        const float2 *base = data + (int64_t)kyy * rs + kz;
+        const int64_t es = (int64_t)N * rs;
+        float2 v[8];
+#pragma unroll
+        for (int s = 0; s < 8; ++s)
+            v[s] = valid ? __ldcs(base + (int64_t)(t + s * P) * es) : make_float2(0.f, 0.f);
+        fft_line<N, -1>(v, t, line, tw);
+        if (valid) {
+            const int ky = kyy > MID ? kyy - N : kyy;
+            const float wyz = win[kyy] * win[kz];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int kxx = t + u * P;
+                bin_mode<WHAT>(H, acc, v[u], kxx, ky, kz, N, axis, win[kxx], wyz, MID);
+            }
+        }
+        if (++since_fold == fold_every) {
+            since_fold = 0;
+            __syncthreads();
+            H.fold();
+        }
+        __syncthreads();   // the shared lines are reused by the next item
+    }
+    __syncthreads();
+    H.fold();
+    __syncthreads();
+    H.flush(acc, MID, WHAT);
+}
+
+template <typename K>
+int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
+    if (bytes > 48 * 1024)
+        PYL_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bytes));
+    return PYL_OK;
+}
+
+template <int N>
+int rows_r2c_n(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int ostride,
+               const float2 *tw) {
+    using CF = RowsCfg<N>;
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * Pow2<N>::LINE);
+    int st;
+    if ((st = set_smem(ctx, k_rows_r2c_p2<N>, smem))) return st;
+    const int64_t pairs = (rows + 1) / 2;
+    const int64_t grid = (pairs + CF::L - 1) / CF::L;
+    k_rows_r2c_p2<N><<<(unsigned)grid, CF::THREADS, smem, ctx->stream>>>(in, out, rows, ostride, tw);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
+}
+
+template <int N>
+int rows_c2r_n(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int istride,
+               const float2 *tw, float scale) {
+    using CF = RowsCfg<N>;
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * Pow2<N>::LINE);
+    int st;
+    if ((st = set_smem(ctx, k_rows_c2r_p2<N>, smem))) return st;
+    const int64_t pairs = (rows + 1) / 2;
+    const int64_t grid = (pairs + CF::L - 1) / CF::L;
+    k_rows_c2r_p2<N><<<(unsigned)grid, CF::THREADS, smem, ctx->stream>>>(in, out, rows, istride,
+                                                                       tw, scale);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
+}
+
+template <int N>
+int cols_n(pyl_ctx *ctx, float2 *data, int ncol, int64_t estride, int64_t ostride, int nouter,
+           int dir, const float2 *tw) {
+    using CF = ColsCfg<N>;
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * Pow2<N>::LINE);
+    int st;
+    dim3 grid((ncol + CF::C - 1) / CF::C, nouter);
+    if (dir < 0) {
+        if ((st = set_smem(ctx, k_cols_p2<N, -1>, smem))) return st;
+        k_cols_p2<N, -1><<<grid, CF::THREADS, smem, ctx->stream>>>(data, ncol, estride, ostride, tw);
+    } else {
+        if ((st = set_smem(ctx, k_cols_p2<N, +1>, smem))) return st;
+        k_cols_p2<N, +1><<<grid, CF::THREADS, smem, ctx->stream>>>(data, ncol, estride, ostride, tw);
+    }
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
+}
+
+template <int N, int WHAT>
+int pk_n(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const float2 *tw,
+         const float *win, int kmax, const PkAcc &acc) {
+    using CF = ColsCfg<N>;
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * Pow2<N>::LINE) +
+                        sizeof(float) * N + BinHist::bytes(kmax, N / 2, WHAT);
+    if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "Pk histogram too large");
+    int st;
+    if ((st = set_smem(ctx, k_pk_x_p2<N, WHAT>, smem))) return st;
+    int per_sm = 0;
+    PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pk_x_p2<N, WHAT>,
+                                                               CF::THREADS, smem));
+    int sms = 0;
+    PYL_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int nitems = N * ((h + CF::C - 1) / CF::C);
+    int grid = (per_sm > 0 ? per_sm : 1) * sms;
+    if (grid > nitems) grid = nitems;
+    k_pk_x_p2<N, WHAT><<<grid, CF::THREADS, smem, ctx->stream>>>(data, h, rs, tw, win, axis, kmax,
+                                                                 acc, nitems, 4);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
+}
+
+template <int N>
+int pk_what(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const float2 *tw,
+            const float *win, int kmax, const PkAcc &acc, int what) {
+    switch (what & PYL_PK_ALL) {
+        case 0: return pk_n<N, 0>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        case 1: return pk_n<N, 1>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        case 2: return pk_n<N, 2>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        case 3: return pk_n<N, 3>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        case 4: return pk_n<N, 4>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        case 5: return pk_n<N, 5>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        case 6: return pk_n<N, 6>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+        default: return pk_n<N, 7>(ctx, data, h, rs, axis, tw, win, kmax, acc);
+    }
+}
+
+}  // namespace
+
+bool pow2_supported(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
+
+#define PYL_POW2_DISPATCH(n, CALL)                 \
+    switch (n) {                                   \
+        case 16: return CALL(16);                  \
+        case 32: return CALL(32);                  \
+        case 64: return CALL(64);                  \
+        case 128: return CALL(128);                \
+        case 256: return CALL(256);                \
+        case 512: return CALL(512);                \
+        case 1024: return CALL(1024);              \
+        case 2048: return CALL(2048);              \
+        case 4096: return CALL(4096);              \
+        default: return PYL_ERR_UNSUPPORTED;       \
+    }
+
+int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
+                  const float2 *tw) {
+#define CALL(N) rows_r2c_n<N>(ctx, in, out, rows, ostride, tw)
+    PYL_POW2_DISPATCH(n, CALL)
+#undef CALL
+}
+
+int pow2_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n, int istride,
+                  const float2 *tw, float scale) {
+#define CALL(N) rows_c2r_n<N>(ctx, in, out, rows, istride, tw, scale)
+    PYL_POW2_DISPATCH(n, CALL)
+#undef CALL
+}
+
+int pow2_cols(pyl_ctx *ctx, float2 *data, int n, int ncol, int64_t estride, int64_t ostride,
+              int nouter, int dir, const float2 *tw) {
+#define CALL(N) cols_n<N>(ctx, data, ncol, estride, ostride, nouter, dir, tw)
+    PYL_POW2_DISPATCH(n, CALL)
+#undef CALL
+}
+
+int pow2_pk_x(pyl_ctx *ctx, const float2 *data, int n, int rs, int axis, const float2 *tw,
+              const float *win, int kmax, const PkAcc &acc, int what) {
+    const int h = n / 2 + 1;
+#define CALL(N) pk_what<N>(ctx, data, h, rs, axis, tw, win, kmax, acc, what)
+    PYL_POW2_DISPATCH(n, CALL)
+#undef CALL
+}
+
+}  // namespace pyl

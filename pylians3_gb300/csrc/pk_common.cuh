@@ -1,0 +1,105 @@
+// Per-mode work of the power-spectrum pass and its per-CTA histograms,
+// shared by the power-of-two and the generic kernels.  Restates the body of
+// the mode loop of class Pk (library/Pk_library/Pk_library.pyx:311-378).
+#pragma once
+
+#include "common.cuh"
+
+namespace pyl {
+
+__device__ __forceinline__ int isqrt_dev(int v) {
+    int r = (int)sqrtf((float)v);
+    while (r * r > v) --r;
+    while ((r + 1) * (r + 1) <= v) ++r;
+    return r;
+}
+
+// Shared-memory histograms of one CTA: float32 bins updated with shared
+// atomics, folded into float64 bins (owner-computes, no atomics) every few
+// items, and added to the global float64 sums once at the end.
+struct BinHist {
+    float *h3, *h1, *hph;    // 3*(kmax+1), mid+1, kmax+1
+    double *d3, *d1, *dph;
+    int n3, n1, nph;
+
+    __host__ __device__ static int count1(int mid, int what) { return (what & PYL_PK_1D) ? mid + 1 : 0; }
+    __host__ __device__ static int countph(int kmax, int what) { return (what & PYL_PK_PHASE) ? kmax + 1 : 0; }
+    __host__ static size_t bytes(int kmax, int mid, int what) {
+        const size_t n = 3 * (size_t)(kmax + 1) + count1(mid, what) + countph(kmax, what);
+        return 8 + n * (sizeof(double) + sizeof(float));
+    }
+    __device__ void setup(void *base, int kmax, int mid, int what) {
+        uintptr_t p = ((uintptr_t)base + 7) & ~(uintptr_t)7;
+        n3 = 3 * (kmax + 1);
+        n1 = count1(mid, what);
+        nph = countph(kmax, what);
+        d3 = (double *)p;
+        d1 = d3 + n3;
+        dph = d1 + n1;
+        h3 = (float *)(dph + nph);
+        h1 = h3 + n3;
+        hph = h1 + n1;
+    }
+    __device__ void zero_all() {
+        const int n = n3 + n1 + nph;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) { d3[i] = 0.0; h3[i] = 0.f; }
+    }
+    // d += h; h = 0   (the arrays are contiguous: one loop covers all three)
+    __device__ void fold() {
+        const int n = n3 + n1 + nph;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const float v = h3[i];
+            if (v != 0.f) { d3[i] += (double)v; h3[i] = 0.f; }
+        }
+    }
+    __device__ void flush(const PkAcc &acc, int mid, int what) {
+        for (int i = threadIdx.x; i < n3; i += blockDim.x)
+            if (d3[i] != 0.0) atomicAdd(&acc.P3[i], d3[i]);
+        for (int i = threadIdx.x; i < n1; i += blockDim.x)
+            if (d1[i] != 0.0) atomicAdd(&acc.P1[i], d1[i]);
+        for (int i = threadIdx.x; i < nph; i += blockDim.x)
+            if (dph[i] != 0.0) atomicAdd(&acc.Pph[i], dph[i]);
+    }
+};
+
+// One independent mode (kxx, ky, kz) with raw value v: Hermitian half-space
+// selection (:324-327), |k| bin = floor(sqrt(kx^2 + ky^2 + kz^2)) exactly,
+// window f = w(kx) w(ky) w(kz) in float32 applied to the complex64 mode
+// (:351-352), |delta|^2 and the Legendre weights of mu^2 = k_par^2 / k^2
+// (:355-375).  wx = w(kx), wyz = w(ky) w(kz).
+template <int WHAT>
+__device__ __forceinline__ void bin_mode(BinHist &H, const PkAcc &acc, float2 v, int kxx, int ky,
+                                         int kz, int n, int axis, float wx, float wyz, int mid) {
+    const bool even = (n & 1) == 0;
+    const int kx = kxx > mid ? kxx - n : kxx;
+    if (kz == 0 || (kz == mid && even)) {
+        if (kx < 0) return;
+        if (kx == 0 || (kx == mid && even)) {
+            if (ky < 0) return;
+        }
+    }
+    if (kx == 0 && ky == 0 && kz == 0) *acc.dc = v;
+    const int n2 = kx * kx + ky * ky + kz * kz;
+    const int bin = isqrt_dev(n2);
+    const int kpar = axis == 0 ? kx : (axis == 1 ? ky : kz);
+    const float f = wx * wyz;
+    const float re = v.x * f, im = v.y * f;
+    const float d2 = re * re + im * im;
+    const float mu2 = n2 > 0 ? (float)(kpar * kpar) / (float)n2 : 0.f;
+    atomicAdd(&H.h3[3 * bin + 0], d2);
+    atomicAdd(&H.h3[3 * bin + 1], d2 * (3.f * mu2 - 1.f) * 0.5f);
+    atomicAdd(&H.h3[3 * bin + 2], d2 * ((35.f * mu2 - 30.f) * mu2 + 3.f) * 0.125f);
+    if (WHAT & PYL_PK_1D) {
+        if (n2 <= mid * mid) atomicAdd(&H.h1[abs(kpar)], d2);
+    }
+    if (WHAT & PYL_PK_PHASE) {
+        const float ph = atan2f(re, sqrtf(d2));
+        atomicAdd(&H.hph[bin], ph * ph);
+    }
+    if (WHAT & PYL_PK_2D) {
+        const int kper = isqrt_dev(n2 - kpar * kpar);
+        atomicAdd(&acc.P2D[(long long)(mid + 1) * kper + abs(kpar)], (double)d2);
+    }
+}
+
+}  // namespace pyl
