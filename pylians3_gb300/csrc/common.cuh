@@ -47,6 +47,8 @@ struct PkAcc {
     double *Pph = nullptr;    // kmax+1       sum of phase^2
     double *P2D = nullptr;    // (kmax_par+1)*(kmax_per+1)
     float2 *dc = nullptr;     // the raw (k=0) mode, for the grid mean
+    double *mass = nullptr;   // total deposited mass (particles path)
+    float *shift = nullptr;   // constant subtracted from the grid before the FFT
 };
 
 }  // namespace pyl
@@ -137,7 +139,11 @@ inline int scale_any(pyl_ctx *ctx, double *g, int64_t c, double s) {
 // fft.cu (power-of-two lengths go to fft_pow2.cu)
 // r2c along the last axis of rows (rows x n real -> rows x (n/2+1) complex,
 // output row stride ostride >= n/2+1; padding needs a power-of-two n)
-int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride);
+// output row stride ostride >= n/2+1; padding needs a power-of-two n).  When
+// shift is not null, *shift (device) is subtracted from every input value
+// (changes only the k = 0 mode, and keeps its round-off out of the others).
+int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
+                 const float *shift = nullptr);
 // c2r along the last axis, times `scale` (input row stride istride)
 int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n, int istride,
                  float scale);
@@ -148,7 +154,10 @@ int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int
 // fft_pow2.cu
 bool pow2_supported(int n);
 int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
-                  const float2 *tw);
+                  const float2 *tw, const float *shift);
+// total mass (sum of W, or n) into *mass, then *shift = mass / cells
+int mass_and_shift(pyl_ctx *ctx, const float *W, int64_t n, double cells, double *mass,
+                   float *shift);
 int pow2_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n, int istride,
                   const float2 *tw, float scale);
 int pow2_cols(pyl_ctx *ctx, float2 *data, int n, int ncol, int64_t estride, int64_t ostride,

@@ -491,13 +491,25 @@ PkAcc acc_view(void *base, const AccLayout &L) {
     a.Pph = a.P1 + L.n1;
     a.P2D = a.Pph + L.nph;
     a.dc = (float2 *)(a.P2D + L.n2);
+    a.mass = (double *)(a.dc + 1);
+    a.shift = (float *)(a.mass + 1);
     return a;
 }
+
+// Particle info for the fused particles -> spectrum path: the grid holds
+// the deposited density rho; the FFT input is rho - shift with shift the
+// mass per cell, so the large k = 0 term does not enter the other modes'
+// round-off.
+struct MassInfo {
+    const float *W;
+    int64_t n;
+};
 
 // z-r2c and y-c2c of a device grid into the half-complex workspace, then the
 // fused x pass; sums are left in acc (device).
 int pk_device(pyl_ctx *ctx, const float *dgrid, int dims, int axis, int mas, int what,
-              const ModeTables &T, void **acc_out, AccLayout &L) {
+              const ModeTables &T, void **acc_out, AccLayout &L,
+              const MassInfo *mi = nullptr) {
     int st = PYL_OK;
     const int h = dims / 2 + 1;
     const int rs = half_stride(dims);   // padded rows: 64-byte aligned column blocks
@@ -508,9 +520,16 @@ int pk_device(pyl_ctx *ctx, const float *dgrid, int dims, int axis, int mas, int
     void *acc = ws_get(ctx, "pk_acc", L.bytes(), &st);
     if (!acc) return st;
     PYL_CUDA(ctx, cudaMemsetAsync(acc, 0, L.bytes(), ctx->stream));
+    const PkAcc A = acc_view(acc, L);
+    if (mi) {
+        const double cells = (double)dims * dims * dims;
+        if ((st = mass_and_shift(ctx, mi->W, mi->n, cells, A.mass, A.shift))) return st;
+    }
     {
         StageScope s(ctx, ST_FFT_Z);
-        if ((st = fft_rows_r2c(ctx, dgrid, half, (long long)dims * dims, dims, rs))) return st;
+        if ((st = fft_rows_r2c(ctx, dgrid, half, (long long)dims * dims, dims, rs,
+                               mi ? A.shift : nullptr)))
+            return st;
     }
     {
         StageScope s(ctx, ST_FFT_Y);
@@ -588,17 +607,19 @@ int finalize(pyl_ctx *ctx, const ModeTables &T, const std::vector<double> &raw,
     return PYL_OK;
 }
 
+// Sums, the raw k = 0 mode and the deposited mass back to the host.
 int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double> &raw,
-                 float2 *dc) {
+                 float2 *dc, double *mass) {
     raw.resize(L.n3 + L.n1 + L.nph + L.n2 + 8);
+    const size_t sums = sizeof(double) * (L.n3 + L.n1 + L.nph + L.n2);
     {
         StageScope s(ctx, ST_D2H);
-        PYL_CUDA(ctx, cudaMemcpyAsync(raw.data(), acc, L.bytes() - 64 + sizeof(float2),
+        PYL_CUDA(ctx, cudaMemcpyAsync(raw.data(), acc, sums + sizeof(float2) + sizeof(double),
                                       cudaMemcpyDeviceToHost, ctx->stream));
     }
     PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    memcpy(dc, (const char *)raw.data() + sizeof(double) * (L.n3 + L.n1 + L.nph + L.n2),
-           sizeof(float2));
+    memcpy(dc, (const char *)raw.data() + sums, sizeof(float2));
+    memcpy(mass, (const char *)raw.data() + sums + sizeof(float2), sizeof(double));
     return PYL_OK;
 }
 
@@ -627,7 +648,8 @@ int pyl_pk(pyl_ctx *ctx, const float *delta, int dims, double BoxSize, int axis,
     if ((st = pk_device(ctx, dgrid, dims, axis, mas, what, *T, &acc, L))) return st;
     std::vector<double> raw;
     float2 dc;
-    if ((st = download_raw(ctx, acc, L, raw, &dc))) return st;
+    double mass;
+    if ((st = download_raw(ctx, acc, L, raw, &dc, &mass))) return st;
     return finalize(ctx, *T, raw, L, BoxSize, what, 1.0, false, out);
 }
 
@@ -672,12 +694,18 @@ int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n, const float *W, 
     }
     void *acc = nullptr;
     AccLayout L;
-    if ((st = pk_device(ctx, grid, dims, axis, mas_window, what, *T, &acc, L))) return st;
+    const MassInfo mi{dW, n};
+    if ((st = pk_device(ctx, grid, dims, axis, mas_window, what, *T, &acc, L, &mi))) return st;
     std::vector<double> raw;
     float2 dc;
-    if ((st = download_raw(ctx, acc, L, raw, &dc))) return st;
-    // mean of the grid = DC mode / dims^3; P(delta) = P(rho) / mean^2
-    const double mean = (double)dc.x / ((double)dims * dims * dims);
+    double mass;
+    if ((st = download_raw(ctx, acc, L, raw, &dc, &mass))) return st;
+    // The FFT saw rho - shift (shift = mass per cell rounded to float, as on
+    // the device); the grid mean is shift + DC / dims^3, and
+    // P(delta = rho/mean - 1) = P(rho) / mean^2 for every k != 0.
+    const double cells = (double)dims * dims * dims;
+    const double shift = (double)(float)(mass * (1.0 / cells));
+    const double mean = shift + (double)dc.x / cells;
     if (!(mean > 0.0) && !(mean < 0.0))
         return fail(ctx, PYL_ERR_ARG, "grid mean is zero: cannot form the overdensity");
     return finalize(ctx, *T, raw, L, BoxSize, what, 1.0 / (mean * mean), true, out);

@@ -4,16 +4,20 @@
 //
 // Two paths:
 //  * unsorted: one thread per particle, one global float atomic (RED) per
-//    tap.  Used for small inputs, 2D, float64 grids, and inputs whose order is
-//    already spatially coherent enough for L2 to absorb the atomics.
-//  * tile-sorted (3D float32): particles are counting-sorted by the tile of
-//    their home cell (tiles of TX*TY*TZ cells), each tile's footprint
-//    (tile + stencil halo) is accumulated in shared memory with shared
-//    atomics, and the footprint is added to the grid with vectorised global
-//    reductions (red.global.add.v4.f32).  Sort: per-block tile histograms
-//    (block-major chunks of the particle array), one exclusive scan over the
-//    tile-major (tile, block) count matrix, and a scatter whose destination is
-//    offset[tile][block] + a shared-memory cursor -- no global atomics.
+//    tap.  Used for small inputs, 2D and float64 grids.
+//  * tile-sorted (3D float32): particles are sorted by the tile of their
+//    home cell (tiles of TX*TY*TZ cells), each tile's footprint (tile + the
+//    stencil halo) is accumulated in shared memory with shared atomics, and
+//    added to the grid with vectorised global reductions (red.global.add.v4).
+//    The sort is a counting sort done in two partition passes so that every
+//    write to HBM is a contiguous run: pass 1 splits the particles into
+//    "coarse" buckets of F consecutive tiles, pass 2 splits each bucket into
+//    its tiles.  A pass stages KP particles in shared memory, orders them by
+//    key there, reserves one contiguous range per key with a single global
+//    atomic on that key's cursor, and writes each key's run in one go.
+//    Tile start offsets come from a counting pass and an exclusive scan.
+//    Tiles holding very many particles (clusters) are split into several
+//    work items, so one CTA never serialises a dense halo.
 //
 // 2D (coord = 2) follows MA's expand_dims path: the third axis has extent 1,
 // index 0 and weight 1 for every tap, so a particle is deposited 2/3/4 times
@@ -122,176 +126,6 @@ int launch_atomic(pyl_ctx *ctx, const float *pos, long long n, int coord, const 
     return PYL_OK;
 }
 
-// -------------------------------------------------------- tile-sorted path
-struct TileGeom {
-    int dims;
-    int TX, TY, TZ;      // tile extent in cells
-    int ntx, nty, ntz;   // tiles per axis
-    int RX, RY, RZ;      // shared footprint extent = T + LO + HI
-    int ntiles;
-};
-
-template <int MAS>
-__device__ __forceinline__ int tile_of(const float *p, float inv, const TileGeom &g) {
-    const int hx = wrap_idx(home_cell<MAS>(cell_dist(p[0], inv)), g.dims);
-    const int hy = wrap_idx(home_cell<MAS>(cell_dist(p[1], inv)), g.dims);
-    const int hz = wrap_idx(home_cell<MAS>(cell_dist(p[2], inv)), g.dims);
-    return ((hx / g.TX) * g.nty + hy / g.TY) * g.ntz + hz / g.TZ;
-}
-
-// Phase A: per-block tile histograms -> hist[tile * B + block]
-template <int MAS>
-__global__ void __launch_bounds__(1024)
-k_tile_hist(const float *__restrict__ pos, long long n, long long chunk, float inv,
-            TileGeom g, unsigned *__restrict__ hist) {
-    extern __shared__ unsigned s_cnt[];
-    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x) s_cnt[t] = 0u;
-    __syncthreads();
-    const long long b0 = blockIdx.x * chunk;
-    const long long b1 = min(n, b0 + chunk);
-    for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x)
-        atomicAdd(&s_cnt[tile_of<MAS>(pos + 3 * i, inv, g)], 1u);
-    __syncthreads();
-    const int B = gridDim.x;
-    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
-        hist[(size_t)t * B + blockIdx.x] = s_cnt[t];
-}
-
-// Phase C: scatter particles (and weights) to their tile-sorted slots.
-template <int MAS, bool HAS_W>
-__global__ void __launch_bounds__(1024)
-k_tile_scatter(const float *__restrict__ pos, const float *__restrict__ W, long long n,
-               long long chunk, float inv, TileGeom g, const unsigned *__restrict__ off,
-               float *__restrict__ spos, float *__restrict__ sw) {
-    extern __shared__ unsigned s_cur[];
-    const int B = gridDim.x;
-    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
-        s_cur[t] = off[(size_t)t * B + blockIdx.x];
-    __syncthreads();
-    const long long b0 = blockIdx.x * chunk;
-    const long long b1 = min(n, b0 + chunk);
-    for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-        const float x = __ldcs(pos + 3 * i), y = __ldcs(pos + 3 * i + 1),
-                    z = __ldcs(pos + 3 * i + 2);
-        const float p[3] = {x, y, z};
-        const unsigned slot = atomicAdd(&s_cur[tile_of<MAS>(p, inv, g)], 1u);
-        spos[3 * (size_t)slot + 0] = x;
-        spos[3 * (size_t)slot + 1] = y;
-        spos[3 * (size_t)slot + 2] = z;
-        if (HAS_W) sw[slot] = __ldcs(W + i);
-    }
-}
-
-__device__ __forceinline__ void red_v4(float *addr, float a, float b, float c, float d) {
-    asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
-                 :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
-}
-
-// Phase D: one CTA per tile: shared footprint, shared atomics, global flush.
-template <int MAS, bool HAS_W>
-__global__ void __launch_bounds__(512)
-k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
-               const unsigned *__restrict__ off, int B, long long n, float inv, TileGeom g,
-               float *__restrict__ grid, int vec4) {
-    using S = Stencil<MAS>;
-    constexpr int NT = S::NT;
-    extern __shared__ float s_reg[];
-    const int t = blockIdx.x;
-    const int RX = g.RX, RY = g.RY, RZ = g.RZ;
-    const int cells = RX * RY * RZ;
-    for (int i = threadIdx.x; i < cells; i += blockDim.x) s_reg[i] = 0.f;
-    const int tx = t / (g.nty * g.ntz), ty = (t / g.ntz) % g.nty, tz = t % g.ntz;
-    const int ox = tx * g.TX, oy = ty * g.TY, oz = tz * g.TZ;   // tile origin (cells)
-    const long long p0 = off[(size_t)t * B];
-    const long long p1 = (t + 1 < g.ntiles) ? (long long)off[(size_t)(t + 1) * B] : n;
-    __syncthreads();
-    for (long long i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
-        int lx[NT], ly[NT], lz[NT];
-        float wx[NT], wy[NT], wz[NT];
-        {
-            const float d = cell_dist(__ldcs(spos + 3 * i + 0), inv);
-            const int c = home_cell<MAS>(d);
-            const int base = wrap_idx(c, g.dims) - ox + S::LO;
-            int o[NT];
-            axis_stencil<MAS>(d, c, o, wx);
-#pragma unroll
-            for (int j = 0; j < NT; ++j) lx[j] = base + o[j];
-        }
-        {
-            const float d = cell_dist(__ldcs(spos + 3 * i + 1), inv);
-            const int c = home_cell<MAS>(d);
-            const int base = wrap_idx(c, g.dims) - oy + S::LO;
-            int o[NT];
-            axis_stencil<MAS>(d, c, o, wy);
-#pragma unroll
-            for (int j = 0; j < NT; ++j) ly[j] = base + o[j];
-        }
-        {
-            const float d = cell_dist(__ldcs(spos + 3 * i + 2), inv);
-            const int c = home_cell<MAS>(d);
-            const int base = wrap_idx(c, g.dims) - oz + S::LO;
-            int o[NT];
-            axis_stencil<MAS>(d, c, o, wz);
-#pragma unroll
-            for (int j = 0; j < NT; ++j) lz[j] = base + o[j];
-        }
-        const float wt = HAS_W ? __ldcs(sw + i) : 1.f;
-#pragma unroll
-        for (int l = 0; l < NT; ++l) {
-#pragma unroll
-            for (int m = 0; m < NT; ++m) {
-                const float wxy = wx[l] * wy[m];
-                float *row = s_reg + (lx[l] * RY + ly[m]) * RZ;
-#pragma unroll
-                for (int q = 0; q < NT; ++q) {
-                    float v = wxy * wz[q];
-                    if (HAS_W) v *= wt;
-                    atomicAdd(row + lz[q], v);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    const int d = g.dims;
-    const long long dd = (long long)d * d;
-    const int zs = oz - S::LO;  // unwrapped global z of footprint column 0
-    if (vec4) {
-        // quads aligned to the global z index (dims % 4 == 0: never wraps inside)
-        const int q0 = (zs >= 0 ? zs : zs - 3) / 4;          // floor(zs / 4)
-        const int q1 = (zs + RZ - 1 >= 0 ? zs + RZ - 1 : zs + RZ - 4) / 4;
-        const int nq = q1 - q0 + 1;
-        const int work = RX * RY * nq;
-        for (int w = threadIdx.x; w < work; w += blockDim.x) {
-            const int q = w % nq;
-            const int r = w / nq;
-            const int ly = r % RY, lx = r / RY;
-            const int zq = 4 * (q0 + q);                      // unwrapped quad start
-            float v[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int lz = zq + e - zs;
-                v[e] = (lz >= 0 && lz < RZ) ? s_reg[(lx * RY + ly) * RZ + lz] : 0.f;
-            }
-            if (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f) {
-                const int gx = wrap_idx(ox - S::LO + lx, d);
-                const int gy = wrap_idx(oy - S::LO + ly, d);
-                const int gz = wrap_idx(zq, d);
-                red_v4(grid + gx * dd + (long long)gy * d + gz, v[0], v[1], v[2], v[3]);
-            }
-        }
-    } else {
-        for (int c = threadIdx.x; c < cells; c += blockDim.x) {
-            const float v = s_reg[c];
-            if (v == 0.f) continue;
-            const int lz = c % RZ, ly = (c / RZ) % RY, lx = c / (RZ * RY);
-            const int gx = wrap_idx(ox - S::LO + lx, d);
-            const int gy = wrap_idx(oy - S::LO + ly, d);
-            const int gz = wrap_idx(zs + lz, d);
-            atomicAdd(grid + gx * dd + (long long)gy * d + gz, v);
-        }
-    }
-}
-
 // ------------------------------------------------------------------- scan
 // Exclusive scan of a uint32 array in place (three passes: block sums, scan
 // of block sums, block-local scan + offset).
@@ -299,6 +133,8 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 8;
 constexpr int kScanChunk = kScanThreads * kScanPer;
 
+// Block-wide exclusive scan of one value per thread.  Uses s_warp[32]; two
+// consecutive calls must be separated by a __syncthreads().
 __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *s_warp,
                                                          unsigned *total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -390,6 +226,290 @@ int scan_exclusive(pyl_ctx *ctx, unsigned *a, long long n) {
     return PYL_OK;
 }
 
+// -------------------------------------------------------- tile-sorted path
+struct TileGeom {
+    int dims;
+    int TX, TY, TZ;      // tile extent in cells
+    int ntx, nty, ntz;   // tiles per axis
+    int RX, RY, RZ;      // shared footprint extent = T + LO + HI
+    int ntiles;
+    int F;               // tiles per coarse bucket (power of two)
+    int ncoarse;         // coarse buckets = ceil(ntiles / F)
+};
+
+constexpr int KP = 2048;          // particles staged per partition step
+constexpr int kPartThreads = 512;
+constexpr int kMaxKeys = 512;     // buckets of one partition step
+constexpr unsigned kItemCap = 65536;  // particles per deposit work item
+
+template <int MAS>
+__device__ __forceinline__ int tile_of(float x, float y, float z, float inv, const TileGeom &g) {
+    const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
+    const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
+    const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
+    return ((hx / g.TX) * g.nty + hy / g.TY) * g.ntz + hz / g.TZ;
+}
+
+// Counting pass: particles per tile (shared histogram, then global adds).
+template <int MAS>
+__global__ void __launch_bounds__(1024, 1)
+k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
+             unsigned *__restrict__ count) {
+    extern __shared__ unsigned s_cnt[];
+    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x) s_cnt[t] = 0u;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&s_cnt[tile_of<MAS>(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1),
+                                      __ldg(pos + 3 * i + 2), inv, g)], 1u);
+    __syncthreads();
+    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
+        if (s_cnt[t]) atomicAdd(&count[t], s_cnt[t]);
+}
+
+// After the scan (start[0..ntiles] exclusive, start[ntiles] = n): the key
+// cursors of both passes and the deposit work items (tile, chunk) of every
+// non-empty tile, chunk = kItemCap particles.  nchunk is scanned separately.
+__global__ void k_sort_setup(const unsigned *__restrict__ start, int ntiles, int F, int ncoarse,
+                             unsigned *__restrict__ fine_cur, unsigned *__restrict__ coarse_cur,
+                             unsigned *__restrict__ nchunk) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+        fine_cur[t] = start[t];
+        const unsigned cnt = start[t + 1] - start[t];
+        nchunk[t] = (cnt + kItemCap - 1) / kItemCap;
+        if (t % F == 0) coarse_cur[t / F] = start[t];
+    }
+}
+
+__global__ void k_items(const unsigned *__restrict__ nchunk_ex, const unsigned *__restrict__ start,
+                        int ntiles, uint2 *__restrict__ items, unsigned *__restrict__ nitems) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+        const unsigned cnt = start[t + 1] - start[t];
+        const unsigned k = (cnt + kItemCap - 1) / kItemCap;
+        for (unsigned c = 0; c < k; ++c) items[nchunk_ex[t] + c] = make_uint2(t, c);
+        if (t == ntiles - 1) *nitems = nchunk_ex[t] + k;
+    }
+}
+
+// One partition pass.  FINE = false: keys are coarse buckets (tile / F) of
+// the particles in input order; FINE = true: the input is grouped by coarse
+// bucket and each bucket is split into its F tiles.  A CTA owns an input
+// range of KP particles (split at coarse-bucket boundaries in the fine pass).
+template <int MAS, bool HAS_W, bool FINE>
+__global__ void __launch_bounds__(kPartThreads, 2)
+k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
+            float *__restrict__ dst, float *__restrict__ dstw, long long n, float inv,
+            TileGeom g, unsigned *__restrict__ cursor, const unsigned *__restrict__ start) {
+    extern __shared__ float sm[];
+    float *sp = sm;                    // 3*KP staged particles (input order)
+    float *sp2 = sp + 3 * KP;          // 3*KP particles in key order
+    float *sw = sp2 + 3 * KP;          // KP weights (input order)
+    float *sw2 = sw + (HAS_W ? KP : 0);
+    unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + (HAS_W ? KP : 0));
+    unsigned short *skey2 = skey + KP;
+    unsigned *hist = reinterpret_cast<unsigned *>(skey2 + KP);   // kMaxKeys each
+    unsigned *loff = hist + kMaxKeys;
+    unsigned *lcur = loff + kMaxKeys;
+    unsigned *gbase = lcur + kMaxKeys;
+    __shared__ unsigned s_warp[32];
+    __shared__ long long s_seg[2];
+
+    const long long r0 = (long long)blockIdx.x * KP;
+    const long long r1 = min(n, r0 + KP);
+    long long seg0 = r0;
+    while (seg0 < r1) {
+        // ---- segment [seg0, seg1) with keys in [keybase, keybase + nkeys)
+        long long seg1 = r1;
+        int keybase = 0, nkeys = g.ncoarse;
+        if (FINE) {
+            if (threadIdx.x == 0) {
+                // coarse bucket containing position seg0: last c with start[c*F] <= seg0
+                int lo = 0, hi = g.ncoarse - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) / 2;
+                    if ((long long)start[min(mid * g.F, g.ntiles)] <= seg0) lo = mid;
+                    else hi = mid - 1;
+                }
+                const long long bend = start[min((lo + 1) * g.F, g.ntiles)];
+                s_seg[0] = lo;
+                s_seg[1] = bend < r1 ? bend : r1;
+            }
+            __syncthreads();
+            const int c = (int)s_seg[0];
+            seg1 = s_seg[1];
+            keybase = c * g.F;
+            nkeys = min(g.F, g.ntiles - keybase);
+        }
+        const int cnt = (int)(seg1 - seg0);
+        for (int b = threadIdx.x; b < nkeys; b += blockDim.x) hist[b] = 0u;
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const long long q = seg0 + i;
+            const float x = __ldcs(src + 3 * q), y = __ldcs(src + 3 * q + 1),
+                        z = __ldcs(src + 3 * q + 2);
+            const int t = tile_of<MAS>(x, y, z, inv, g);
+            const int key = FINE ? t - keybase : t / g.F;
+            sp[3 * i] = x;
+            sp[3 * i + 1] = y;
+            sp[3 * i + 2] = z;
+            if (HAS_W) sw[i] = __ldcs(srcw + q);
+            skey[i] = (unsigned short)key;
+            atomicAdd(&hist[key], 1u);
+        }
+        __syncthreads();
+        const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
+        const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
+        if (threadIdx.x < nkeys) {
+            loff[threadIdx.x] = ex;
+            lcur[threadIdx.x] = ex;
+            gbase[threadIdx.x] = hv ? atomicAdd(&cursor[keybase + threadIdx.x], hv) : 0u;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const int key = skey[i];
+            const unsigned r = atomicAdd(&lcur[key], 1u);
+            sp2[3 * r] = sp[3 * i];
+            sp2[3 * r + 1] = sp[3 * i + 1];
+            sp2[3 * r + 2] = sp[3 * i + 2];
+            if (HAS_W) sw2[r] = sw[i];
+            skey2[r] = (unsigned short)key;
+        }
+        __syncthreads();
+        // key runs are contiguous both here and in the destination
+        for (int j = threadIdx.x; j < 3 * cnt; j += blockDim.x) {
+            const int e = j / 3;
+            const int key = skey2[e];
+            const size_t d = (size_t)gbase[key] + (e - loff[key]);
+            dst[3 * d + (j - 3 * e)] = sp2[j];
+        }
+        if (HAS_W) {
+            for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+                const int key = skey2[e];
+                dstw[(size_t)gbase[key] + (e - loff[key])] = sw2[e];
+            }
+        }
+        __syncthreads();
+        seg0 = seg1;
+    }
+}
+
+__device__ __forceinline__ void red_v4(float *addr, float a, float b, float c, float d) {
+    asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
+                 :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+
+// Deposit: work items (tile, chunk) over a persistent grid; shared
+// footprint, shared atomics, then a global flush of the footprint.
+template <int MAS, bool HAS_W>
+__global__ void __launch_bounds__(512)
+k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
+               const unsigned *__restrict__ start, const uint2 *__restrict__ items,
+               const unsigned *__restrict__ nitems, float inv, TileGeom g,
+               float *__restrict__ grid, int vec4) {
+    using S = Stencil<MAS>;
+    constexpr int NT = S::NT;
+    extern __shared__ float s_reg[];
+    const int RX = g.RX, RY = g.RY, RZ = g.RZ;
+    const int cells = RX * RY * RZ;
+    const unsigned total = *nitems;
+    for (unsigned it = blockIdx.x; it < total; it += gridDim.x) {
+        const uint2 item = items[it];
+        const int t = (int)item.x;
+        for (int i = threadIdx.x; i < cells; i += blockDim.x) s_reg[i] = 0.f;
+        const int tx = t / (g.nty * g.ntz), ty = (t / g.ntz) % g.nty, tz = t % g.ntz;
+        const int ox = tx * g.TX, oy = ty * g.TY, oz = tz * g.TZ;   // tile origin (cells)
+        const long long p0 = (long long)start[t] + (long long)item.y * kItemCap;
+        const long long p1 = min((long long)start[t + 1], p0 + (long long)kItemCap);
+        __syncthreads();
+        for (long long i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+            int lx[NT], ly[NT], lz[NT];
+            float wx[NT], wy[NT], wz[NT];
+            {
+                const float d = cell_dist(__ldcs(spos + 3 * i + 0), inv);
+                const int c = home_cell<MAS>(d);
+                const int base = wrap_idx(c, g.dims) - ox + S::LO;
+                int o[NT];
+                axis_stencil<MAS>(d, c, o, wx);
+#pragma unroll
+                for (int j = 0; j < NT; ++j) lx[j] = base + o[j];
+            }
+            {
+                const float d = cell_dist(__ldcs(spos + 3 * i + 1), inv);
+                const int c = home_cell<MAS>(d);
+                const int base = wrap_idx(c, g.dims) - oy + S::LO;
+                int o[NT];
+                axis_stencil<MAS>(d, c, o, wy);
+#pragma unroll
+                for (int j = 0; j < NT; ++j) ly[j] = base + o[j];
+            }
+            {
+                const float d = cell_dist(__ldcs(spos + 3 * i + 2), inv);
+                const int c = home_cell<MAS>(d);
+                const int base = wrap_idx(c, g.dims) - oz + S::LO;
+                int o[NT];
+                axis_stencil<MAS>(d, c, o, wz);
+#pragma unroll
+                for (int j = 0; j < NT; ++j) lz[j] = base + o[j];
+            }
+            const float wt = HAS_W ? __ldcs(sw + i) : 1.f;
+#pragma unroll
+            for (int l = 0; l < NT; ++l) {
+#pragma unroll
+                for (int m = 0; m < NT; ++m) {
+                    const float wxy = wx[l] * wy[m];
+                    float *row = s_reg + (lx[l] * RY + ly[m]) * RZ;
+#pragma unroll
+                    for (int q = 0; q < NT; ++q) {
+                        float v = wxy * wz[q];
+                        if (HAS_W) v *= wt;
+                        atomicAdd(row + lz[q], v);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int d = g.dims;
+        const long long dd = (long long)d * d;
+        const int zs = oz - S::LO;  // unwrapped global z of footprint column 0
+        if (vec4) {
+            // quads aligned to the global z index (dims % 4 == 0: never wraps inside)
+            const int q0 = (zs >= 0 ? zs : zs - 3) / 4;          // floor(zs / 4)
+            const int q1 = (zs + RZ - 1 >= 0 ? zs + RZ - 1 : zs + RZ - 4) / 4;
+            const int nq = q1 - q0 + 1;
+            const int work = RX * RY * nq;
+            for (int w = threadIdx.x; w < work; w += blockDim.x) {
+                const int q = w % nq;
+                const int r = w / nq;
+                const int ly = r % RY, lx = r / RY;
+                const int zq = 4 * (q0 + q);                      // unwrapped quad start
+                float v[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int lz = zq + e - zs;
+                    v[e] = (lz >= 0 && lz < RZ) ? s_reg[(lx * RY + ly) * RZ + lz] : 0.f;
+                }
+                if (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f) {
+                    const int gx = wrap_idx(ox - S::LO + lx, d);
+                    const int gy = wrap_idx(oy - S::LO + ly, d);
+                    const int gz = wrap_idx(zq, d);
+                    red_v4(grid + gx * dd + (long long)gy * d + gz, v[0], v[1], v[2], v[3]);
+                }
+            }
+        } else {
+            for (int c = threadIdx.x; c < cells; c += blockDim.x) {
+                const float v = s_reg[c];
+                if (v == 0.f) continue;
+                const int lz = c % RZ, ly = (c / RZ) % RY, lx = c / (RZ * RY);
+                const int gx = wrap_idx(ox - S::LO + lx, d);
+                const int gy = wrap_idx(oy - S::LO + ly, d);
+                const int gz = wrap_idx(zs + lz, d);
+                atomicAdd(grid + gx * dd + (long long)gy * d + gz, v);
+            }
+        }
+        __syncthreads();   // the footprint is zeroed again by the next item
+    }
+}
+
 template <typename K>
 int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
     if (bytes > 48 * 1024)
@@ -422,63 +542,105 @@ TileGeom make_geom(int dims, int mas) {
     g.RX = g.TX + lo + hi;
     g.RY = g.TY + lo + hi;
     g.RZ = g.TZ + lo + hi;
+    // coarse buckets: ~sqrt(ntiles) tiles each, at most kMaxKeys buckets
+    g.F = 1;
+    while ((long long)g.F * g.F < g.ntiles) g.F *= 2;
+    while ((g.ntiles + g.F - 1) / g.F > kMaxKeys) g.F *= 2;
+    if (g.F > kMaxKeys) g.F = kMaxKeys;
+    g.ncoarse = (g.ntiles + g.F - 1) / g.F;
     return g;
+}
+
+size_t partition_smem(bool weighted) {
+    return sizeof(float) * (6 * (size_t)KP + (weighted ? 2 * (size_t)KP : 0)) +
+           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 4 * kMaxKeys;
+}
+
+template <int MAS, bool HAS_W>
+int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
+                    int dims, float inv, const TileGeom &g) {
+    int st = PYL_OK;
+    const int nt = g.ntiles;
+    // device scratch: counts/starts (nt+1), cursors, item bookkeeping
+    unsigned *start = (unsigned *)ws_get(ctx, "dep_start", sizeof(unsigned) * (size_t)(nt + 1), &st);
+    if (!start) return st;
+    unsigned *fcur = (unsigned *)ws_get(ctx, "dep_fcur", sizeof(unsigned) * (size_t)nt, &st);
+    if (!fcur) return st;
+    unsigned *ccur = (unsigned *)ws_get(ctx, "dep_ccur", sizeof(unsigned) * (size_t)g.ncoarse, &st);
+    if (!ccur) return st;
+    unsigned *nchunk = (unsigned *)ws_get(ctx, "dep_nchunk", sizeof(unsigned) * (size_t)(nt + 1), &st);
+    if (!nchunk) return st;
+    const size_t max_items = (size_t)nt + (size_t)(n / kItemCap) + 1;
+    uint2 *items = (uint2 *)ws_get(ctx, "dep_items", sizeof(uint2) * max_items, &st);
+    if (!items) return st;
+    unsigned *nitems = (unsigned *)ws_get(ctx, "dep_nitems", sizeof(unsigned), &st);
+    if (!nitems) return st;
+    float *b1 = (float *)ws_get(ctx, "dep_b1", sizeof(float) * 3 * (size_t)n, &st);
+    if (!b1) return st;
+    float *b2 = (float *)ws_get(ctx, "dep_b2", sizeof(float) * 3 * (size_t)n, &st);
+    if (!b2) return st;
+    float *w1 = nullptr, *w2 = nullptr;
+    if (HAS_W) {
+        w1 = (float *)ws_get(ctx, "dep_w1", sizeof(float) * (size_t)n, &st);
+        if (!w1) return st;
+        w2 = (float *)ws_get(ctx, "dep_w2", sizeof(float) * (size_t)n, &st);
+        if (!w2) return st;
+    }
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    {
+        StageScope s(ctx, ST_SORT);
+        PYL_CUDA(ctx, cudaMemsetAsync(start, 0, sizeof(unsigned) * (size_t)(nt + 1), ctx->stream));
+        const size_t hsm = sizeof(unsigned) * (size_t)nt;
+        if ((st = set_smem(ctx, k_tile_count<MAS>, hsm))) return st;
+        k_tile_count<MAS><<<sms, 1024, hsm, ctx->stream>>>(pos, n, inv, g, start);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+        // exclusive scan over nt+1 entries (the extra 0 becomes the total n)
+        if ((st = scan_exclusive(ctx, start, nt + 1))) return st;
+        k_sort_setup<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(start, nt, g.F, g.ncoarse, fcur,
+                                                                ccur, nchunk);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+        PYL_CUDA(ctx, cudaMemsetAsync(nchunk + nt, 0, sizeof(unsigned), ctx->stream));
+        if ((st = scan_exclusive(ctx, nchunk, nt + 1))) return st;
+        k_items<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(nchunk, start, nt, items, nitems);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+        const size_t psm = partition_smem(HAS_W);
+        const long long nblk = (n + KP - 1) / KP;
+        if ((st = set_smem(ctx, k_partition<MAS, HAS_W, false>, psm))) return st;
+        k_partition<MAS, HAS_W, false><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
+            pos, W, b1, w1, n, inv, g, ccur, start);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+        if ((st = set_smem(ctx, k_partition<MAS, HAS_W, true>, psm))) return st;
+        k_partition<MAS, HAS_W, true><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
+            b1, w1, b2, w2, n, inv, g, fcur, start);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+    }
+    const int vec4 = (dims % 4 == 0 && ((uintptr_t)grid & 15) == 0) ? 1 : 0;
+    const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
+    if ((st = set_smem(ctx, k_tile_deposit<MAS, HAS_W>, rsm))) return st;
+    int per_sm = 0;
+    PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_deposit<MAS, HAS_W>,
+                                                               512, rsm));
+    long long grid_n = (long long)(per_sm > 0 ? per_sm : 1) * sms * 4;
+    if (grid_n > (long long)max_items) grid_n = (long long)max_items;
+    k_tile_deposit<MAS, HAS_W><<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(
+        b2, w2, start, items, nitems, inv, g, grid, vec4);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
 }
 
 template <int MAS>
 int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
                   int dims, float inv) {
     const TileGeom g = make_geom(dims, MAS);
-    int st = PYL_OK;
-    int B = 4 * 152;
-    long long chunk = (n + B - 1) / B;
-    if (chunk < 1024) { chunk = 1024; B = (int)((n + chunk - 1) / chunk); }
-    const size_t hsm = sizeof(unsigned) * (size_t)g.ntiles;
-    const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
-    const long long nh = (long long)g.ntiles * B;
-    unsigned *hist = (unsigned *)ws_get(ctx, "dep_hist", sizeof(unsigned) * (size_t)nh, &st);
-    if (!hist) return st;
-    float *spos = (float *)ws_get(ctx, "dep_spos", sizeof(float) * 3 * (size_t)n, &st);
-    if (!spos) return st;
-    float *sw = nullptr;
-    if (W) {
-        sw = (float *)ws_get(ctx, "dep_sw", sizeof(float) * (size_t)n, &st);
-        if (!sw) return st;
-    }
-    {
-        StageScope s(ctx, ST_SORT);
-        if ((st = set_smem(ctx, k_tile_hist<MAS>, hsm))) return st;
-        k_tile_hist<MAS><<<B, 1024, hsm, ctx->stream>>>(pos, n, chunk, inv, g, hist);
-        ctx->launches++;
-        PYL_CUDA(ctx, cudaGetLastError());
-        if ((st = scan_exclusive(ctx, hist, nh))) return st;
-        if (W) {
-            if ((st = set_smem(ctx, k_tile_scatter<MAS, true>, hsm))) return st;
-            k_tile_scatter<MAS, true><<<B, 1024, hsm, ctx->stream>>>(pos, W, n, chunk, inv, g,
-                                                                     hist, spos, sw);
-        } else {
-            if ((st = set_smem(ctx, k_tile_scatter<MAS, false>, hsm))) return st;
-            k_tile_scatter<MAS, false><<<B, 1024, hsm, ctx->stream>>>(pos, W, n, chunk, inv, g,
-                                                                      hist, spos, sw);
-        }
-        ctx->launches++;
-        PYL_CUDA(ctx, cudaGetLastError());
-    }
-    // vector reductions need 16-byte aligned quads: dims % 4 == 0 and an
-    // aligned grid base (a user tensor may be a view with an offset)
-    const int vec4 = (dims % 4 == 0 && ((uintptr_t)grid & 15) == 0) ? 1 : 0;
-    if (W) {
-        if ((st = set_smem(ctx, k_tile_deposit<MAS, true>, rsm))) return st;
-        k_tile_deposit<MAS, true><<<g.ntiles, 512, rsm, ctx->stream>>>(spos, sw, hist, B, n, inv,
-                                                                       g, grid, vec4);
-    } else {
-        if ((st = set_smem(ctx, k_tile_deposit<MAS, false>, rsm))) return st;
-        k_tile_deposit<MAS, false><<<g.ntiles, 512, rsm, ctx->stream>>>(spos, sw, hist, B, n,
-                                                                        inv, g, grid, vec4);
-    }
-    ctx->launches++;
-    PYL_CUDA(ctx, cudaGetLastError());
-    return PYL_OK;
+    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g)
+             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g);
 }
 
 bool use_sorted(long long n, int coord, int dims, int mas, int flags) {
@@ -487,7 +649,7 @@ bool use_sorted(long long n, int coord, int dims, int mas, int flags) {
     const TileGeom g = make_geom(dims, mas);
     const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
     if (rsm > 200 * 1024 || (size_t)g.ntiles * 4 > 200 * 1024) return false;
-    if ((long long)g.ntiles * 4 * 152 >= (1LL << 31)) return false;
+    if (g.F > 65535 || g.ncoarse > kMaxKeys) return false;
     if (n >= (1LL << 32) - 1) return false;
     if (flags & PYL_DEPOSIT_SORTED) return true;
     return n >= (1LL << 20) && dims >= 32;
@@ -532,6 +694,42 @@ int deposit_f64(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const floa
 
 int scale_grid(pyl_ctx *ctx, float *grid, int64_t count, float s) {
     return scale_t<float>(ctx, grid, count, s);
+}
+
+namespace {
+
+__global__ void __launch_bounds__(256)
+k_wsum(const float *__restrict__ W, long long n, double *__restrict__ mass) {
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        s += (double)W[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(mass, s);
+}
+
+__global__ void k_shift(double *mass, long long n, int weighted, double inv_cells,
+                        float *shift) {
+    if (!weighted) *mass = (double)n;
+    *shift = (float)(*mass * inv_cells);
+}
+
+}  // namespace
+
+int mass_and_shift(pyl_ctx *ctx, const float *W, int64_t n, double cells, double *mass,
+                   float *shift) {
+    if (W) {
+        long long blocks = (n + 255) / 256;
+        if (blocks > 152LL * 8) blocks = 152LL * 8;
+        if (blocks < 1) blocks = 1;
+        k_wsum<<<(unsigned)blocks, 256, 0, ctx->stream>>>(W, n, mass);
+        ctx->launches++;
+    }
+    k_shift<<<1, 1, 0, ctx->stream>>>(mass, n, W ? 1 : 0, 1.0 / cells, shift);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
 }
 
 int scale_grid_f64(pyl_ctx *ctx, double *grid, int64_t count, double s) {

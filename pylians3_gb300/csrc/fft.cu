@@ -22,7 +22,8 @@ constexpr size_t kLineBudget = 64 * 1024;  // bytes of one line buffer per CTA
 template <int DIR>
 __global__ void __launch_bounds__(kThreads)
 k_rows_r2c(const float *__restrict__ in, float2 *__restrict__ out, int64_t rows,
-           FftDesc D, const float2 *__restrict__ g_tw, int pairs) {
+           FftDesc D, const float2 *__restrict__ g_tw, int pairs,
+           const float *__restrict__ shift) {
     extern __shared__ float2 sm[];
     const int n = D.n;
     const int h = n / 2 + 1;
@@ -30,12 +31,13 @@ k_rows_r2c(const float *__restrict__ in, float2 *__restrict__ out, int64_t rows,
     float2 *b0 = tw + n;
     float2 *b1 = b0 + (size_t)pairs * n;
     load_twiddles(tw, g_tw, n);
+    const float sh = shift ? *shift : 0.f;
     const long long row0 = (long long)blockIdx.x * pairs * 2;
     for (int idx = threadIdx.x; idx < pairs * n; idx += blockDim.x) {
         const int p = idx / n, i = idx - p * n;
         const long long ra = row0 + 2 * p, rb = ra + 1;
-        const float a = ra < rows ? __ldcs(in + ra * n + i) : 0.f;
-        const float b = rb < rows ? __ldcs(in + rb * n + i) : 0.f;
+        const float a = ra < rows ? __ldcs(in + ra * n + i) - sh : 0.f;
+        const float b = rb < rows ? __ldcs(in + rb * n + i) - sh : 0.f;
         b0[idx] = make_float2(a, b);
     }
     __syncthreads();
@@ -126,11 +128,11 @@ int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
 }  // namespace
 
 int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n,
-                 int ostride) {
+                 int ostride, const float *shift) {
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
-    if (pow2_supported(n)) return pow2_rows_r2c(ctx, in, out, rows, n, ostride, P->d_tw);
+    if (pow2_supported(n)) return pow2_rows_r2c(ctx, in, out, rows, n, ostride, P->d_tw, shift);
     if (ostride != n / 2 + 1) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     int pairs = (int)(kLineBudget / (sizeof(float2) * (size_t)n));
     if (pairs < 1) pairs = 1;
@@ -141,7 +143,7 @@ int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n
     if ((st = set_smem(ctx, k_rows_r2c<-1>, smem))) return st;
     const int64_t grid = (npairs + pairs - 1) / pairs;
     k_rows_r2c<-1><<<(unsigned)grid, kThreads, smem, ctx->stream>>>(in, out, rows, P->desc,
-                                                                  P->d_tw, pairs);
+                                                                  P->d_tw, pairs, shift);
     ctx->launches++;
     PYL_CUDA(ctx, cudaGetLastError());
     return PYL_OK;

@@ -38,7 +38,7 @@ struct ColsCfg {
 template <int N>
 __global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
 k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t rows, int ostride,
-              const float2 *__restrict__ g_tw) {
+              const float2 *__restrict__ g_tw, const float *__restrict__ shift) {
     using CF = RowsCfg<N>;
     constexpr int P = CF::P, LINE = Pow2<N>::LINE, H = N / 2 + 1;
     extern __shared__ float2 sm[];
@@ -46,12 +46,13 @@ k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t ro
     const int l = threadIdx.x / P, t = threadIdx.x % P;
     float2 *line = sm + N + l * LINE;
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    const float sh = shift ? *shift : 0.f;
     const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
     float2 v[8];
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
-        const float a = ra < rows ? __ldcs(in + ra * N + t + s * P) : 0.f;
-        const float b = rb < rows ? __ldcs(in + rb * N + t + s * P) : 0.f;
+        const float a = ra < rows ? __ldcs(in + ra * N + t + s * P) - sh : 0.f;
+        const float b = rb < rows ? __ldcs(in + rb * N + t + s * P) - sh : 0.f;
         v[s] = make_float2(a, b);
     }
     __syncthreads();
@@ -162,13 +163,26 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
         for (int s = 0; s < 8; ++s)
             v[s] = valid ? __ldcs(base + (int64_t)(t + s * P) * es) : make_float2(0.f, 0.f);
         fft_line<N, -1>(v, t, line, tw);
-        if (valid) {
-            const int ky = kyy > MID ? kyy - N : kyy;
-            const float wyz = win[kyy] * win[kz];
+        // natural order into the line, then each thread bins a run of 8
+        // consecutive kx of one column (neighbouring lanes -> different bins)
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int kxx = t + u * P;
-                bin_mode<WHAT>(H, acc, v[u], kxx, ky, kz, N, axis, win[kxx], wyz, MID);
+        for (int u = 0; u < 8; ++u) line[pad8(t + u * P)] = v[u];
+        __syncthreads();
+        {
+            const int cc = threadIdx.x / P, rr = threadIdx.x % P;
+            const int kzc = (it % nzb) * C + cc;
+            if (kzc < h) {
+                const float2 *ln = sm + N + cc * LINE;
+                const int ky = kyy > MID ? kyy - N : kyy;
+                const float wyz = win[kyy] * win[kzc];
+                BinRun R;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int kxx = 8 * rr + i;
+                    bin_mode_run<WHAT>(R, H, acc, ln[pad8(kxx)], kxx, ky, kzc, N, axis,
+                                       win[kxx], wyz, MID);
+                }
+                R.flush(H);
             }
         }
         if (++since_fold == fold_every) {
@@ -194,14 +208,15 @@ int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
 
 template <int N>
 int rows_r2c_n(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int ostride,
-               const float2 *tw) {
+               const float2 *tw, const float *shift) {
     using CF = RowsCfg<N>;
     const size_t smem = sizeof(float2) * (N + (size_t)CF::L * Pow2<N>::LINE);
     int st;
     if ((st = set_smem(ctx, k_rows_r2c_p2<N>, smem))) return st;
     const int64_t pairs = (rows + 1) / 2;
     const int64_t grid = (pairs + CF::L - 1) / CF::L;
-    k_rows_r2c_p2<N><<<(unsigned)grid, CF::THREADS, smem, ctx->stream>>>(in, out, rows, ostride, tw);
+    k_rows_r2c_p2<N><<<(unsigned)grid, CF::THREADS, smem, ctx->stream>>>(in, out, rows, ostride, tw,
+                                                                       shift);
     ctx->launches++;
     PYL_CUDA(ctx, cudaGetLastError());
     return PYL_OK;
@@ -300,8 +315,8 @@ bool pow2_supported(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; 
     }
 
 int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
-                  const float2 *tw) {
-#define CALL(N) rows_r2c_n<N>(ctx, in, out, rows, ostride, tw)
+                  const float2 *tw, const float *shift) {
+#define CALL(N) rows_r2c_n<N>(ctx, in, out, rows, ostride, tw, shift)
     PYL_POW2_DISPATCH(n, CALL)
 #undef CALL
 }

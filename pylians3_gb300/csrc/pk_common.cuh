@@ -62,6 +62,75 @@ struct BinHist {
     }
 };
 
+// The extra (non-3D) outputs of one mode: 1D and phase into the shared
+// histograms, 2D into the global float64 sums.
+template <int WHAT>
+__device__ __forceinline__ void mode_extras(BinHist &H, const PkAcc &acc, int n2, int bin,
+                                            int kpar, float re, float d2, int mid) {
+    if (WHAT & PYL_PK_1D) {
+        if (n2 <= mid * mid) atomicAdd(&H.h1[abs(kpar)], d2);
+    }
+    if (WHAT & PYL_PK_PHASE) {
+        const float ph = atan2f(re, sqrtf(d2));
+        atomicAdd(&H.hph[bin], ph * ph);
+    }
+    if (WHAT & PYL_PK_2D) {
+        const int kper = isqrt_dev(n2 - kpar * kpar);
+        atomicAdd(&acc.P2D[(long long)(mid + 1) * kper + abs(kpar)], (double)d2);
+    }
+}
+
+// Register run of consecutive modes that fall into the same |k| bin: the
+// three multipole sums are kept in registers and added to the shared
+// histogram once per run.
+struct BinRun {
+    int bin = -1;
+    float p0 = 0.f, p2 = 0.f, p4 = 0.f;
+    __device__ __forceinline__ void flush(BinHist &H) {
+        if (bin >= 0) {
+            atomicAdd(&H.h3[3 * bin + 0], p0);
+            atomicAdd(&H.h3[3 * bin + 1], p2);
+            atomicAdd(&H.h3[3 * bin + 2], p4);
+        }
+        bin = -1;
+        p0 = p2 = p4 = 0.f;
+    }
+    __device__ __forceinline__ void add(BinHist &H, int b, float d2, float mu2) {
+        if (b != bin) {
+            flush(H);
+            bin = b;
+        }
+        p0 += d2;
+        p2 += d2 * (3.f * mu2 - 1.f) * 0.5f;
+        p4 += d2 * ((35.f * mu2 - 30.f) * mu2 + 3.f) * 0.125f;
+    }
+};
+
+// Same per-mode work as bin_mode, accumulating the multipoles into a run.
+template <int WHAT>
+__device__ __forceinline__ void bin_mode_run(BinRun &R, BinHist &H, const PkAcc &acc, float2 v,
+                                             int kxx, int ky, int kz, int n, int axis, float wx,
+                                             float wyz, int mid) {
+    const bool even = (n & 1) == 0;
+    const int kx = kxx > mid ? kxx - n : kxx;
+    if (kz == 0 || (kz == mid && even)) {
+        if (kx < 0) return;
+        if (kx == 0 || (kx == mid && even)) {
+            if (ky < 0) return;
+        }
+    }
+    if (kx == 0 && ky == 0 && kz == 0) *acc.dc = v;
+    const int n2 = kx * kx + ky * ky + kz * kz;
+    const int bin = isqrt_dev(n2);
+    const int kpar = axis == 0 ? kx : (axis == 1 ? ky : kz);
+    const float f = wx * wyz;
+    const float re = v.x * f, im = v.y * f;
+    const float d2 = re * re + im * im;
+    const float mu2 = n2 > 0 ? (float)(kpar * kpar) / (float)n2 : 0.f;
+    R.add(H, bin, d2, mu2);
+    if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
+}
+
 // One independent mode (kxx, ky, kz) with raw value v: Hermitian half-space
 // selection (:324-327), |k| bin = floor(sqrt(kx^2 + ky^2 + kz^2)) exactly,
 // window f = w(kx) w(ky) w(kz) in float32 applied to the complex64 mode
