@@ -229,7 +229,8 @@ int scan_exclusive(pyl_ctx *ctx, unsigned *a, long long n) {
 // -------------------------------------------------------- tile-sorted path
 struct TileGeom {
     int dims;
-    int TX, TY, TZ;      // tile extent in cells
+    int TX, TY, TZ;      // tile extent in cells (powers of two)
+    int sx, sy, sz;      // log2 of the tile extents
     int ntx, nty, ntz;   // tiles per axis
     int RX, RY, RZ;      // shared footprint extent = T + LO + HI
     int ntiles;
@@ -237,9 +238,9 @@ struct TileGeom {
     int ncoarse;         // coarse buckets = ceil(ntiles / F)
 };
 
-constexpr int KP = 2048;          // particles staged per partition step
-constexpr int kPartThreads = 512;
-constexpr int kMaxKeys = 512;     // buckets of one partition step
+constexpr int KP = 1024;          // particles staged per partition step
+constexpr int kPartThreads = 256; // >= kMaxKeys (one scan value per thread)
+constexpr int kMaxKeys = 256;     // buckets of one partition step
 constexpr unsigned kItemCap = 65536;  // particles per deposit work item
 
 template <int MAS>
@@ -247,7 +248,7 @@ __device__ __forceinline__ int tile_of(float x, float y, float z, float inv, con
     const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
     const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
     const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
-    return ((hx / g.TX) * g.nty + hy / g.TY) * g.ntz + hz / g.TZ;
+    return ((hx >> g.sx) * g.nty + (hy >> g.sy)) * g.ntz + (hz >> g.sz);
 }
 
 // Counting pass: particles per tile (shared histogram, then global adds).
@@ -296,7 +297,7 @@ __global__ void k_items(const unsigned *__restrict__ nchunk_ex, const unsigned *
 // bucket and each bucket is split into its F tiles.  A CTA owns an input
 // range of KP particles (split at coarse-bucket boundaries in the fine pass).
 template <int MAS, bool HAS_W, bool FINE>
-__global__ void __launch_bounds__(kPartThreads, 2)
+__global__ void __launch_bounds__(kPartThreads, 4)
 k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             float *__restrict__ dst, float *__restrict__ dstw, long long n, float inv,
             TileGeom g, unsigned *__restrict__ cursor, const unsigned *__restrict__ start) {
@@ -521,9 +522,11 @@ int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
 TileGeom make_geom(int dims, int mas) {
     TileGeom g;
     g.dims = dims;
-    g.TZ = dims >= 32 ? 32 : dims;
-    g.TY = dims >= 32 ? 32 : dims;
-    g.TX = dims >= 1024 ? 32 : (dims >= 16 ? 16 : dims);
+    int p2 = 1;   // largest power of two <= dims, at most 32
+    while (p2 * 2 <= dims && p2 < 32) p2 *= 2;
+    g.TZ = p2;
+    g.TY = p2;
+    g.TX = dims >= 1024 ? 32 : (p2 >= 16 ? 16 : p2);
     auto count = [&](TileGeom &q) {
         q.ntx = (dims + q.TX - 1) / q.TX;
         q.nty = (dims + q.TY - 1) / q.TY;
@@ -537,6 +540,10 @@ TileGeom make_geom(int dims, int mas) {
         else g.TX /= 2;
         count(g);
     }
+    auto lg = [](int v) { int s = 0; while ((1 << s) < v) ++s; return s; };
+    g.sx = lg(g.TX);
+    g.sy = lg(g.TY);
+    g.sz = lg(g.TZ);
     const int lo = (mas == PYL_MAS_TSC || mas == PYL_MAS_PCS) ? 1 : 0;
     const int hi = (mas == PYL_MAS_TSC || mas == PYL_MAS_PCS) ? 2 : 1;
     g.RX = g.TX + lo + hi;

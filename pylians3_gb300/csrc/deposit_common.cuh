@@ -30,6 +30,7 @@ struct Stencil {
 };
 
 __device__ __forceinline__ int wrap_idx(int i, int dims) {
+    if ((unsigned)i < (unsigned)dims) return i;   // the common, in-box case
     i %= dims;
     return i < 0 ? i + dims : i;
 }

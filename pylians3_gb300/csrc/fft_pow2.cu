@@ -152,22 +152,28 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
     __syncthreads();
     const int nzb = (h + C - 1) / C;
     int since_fold = 0;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int kyy = it / nzb;
-        const int kz = (it % nzb) * C + c;
+    // column c of item `item`, element s of thread t -> registers
+    auto load = [&](int item, float2 (&v)[8]) {
+        const int kz = (item % nzb) * C + c;
         const bool valid = kz < h;
-        const float2 *base = data + (int64_t)kyy * rs + kz;
+        const float2 *base = data + (int64_t)(item / nzb) * rs + kz;
         const int64_t es = (int64_t)N * rs;
-        float2 v[8];
 #pragma unroll
         for (int s = 0; s < 8; ++s)
             v[s] = valid ? __ldcs(base + (int64_t)(t + s * P) * es) : make_float2(0.f, 0.f);
+    };
+    float2 v[8];
+    if (blockIdx.x < nitems) load(blockIdx.x, v);
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int kyy = it / nzb;
         fft_line<N, -1>(v, t, line, tw);
         // natural order into the line, then each thread bins a run of 8
         // consecutive kx of one column (neighbouring lanes -> different bins)
 #pragma unroll
         for (int u = 0; u < 8; ++u) line[pad8(t + u * P)] = v[u];
         __syncthreads();
+        // the next item's loads are in flight while this one is binned
+        if (it + (int)gridDim.x < nitems) load(it + gridDim.x, v);
         {
             const int cc = threadIdx.x / P, rr = threadIdx.x % P;
             const int kzc = (it % nzb) * C + cc;
