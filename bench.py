@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--mas", default="CIC")
     ap.add_argument("--axis", type=int, default=0)
     ap.add_argument("--positions", default="uniform", choices=["uniform", "zeldovich"])
+    ap.add_argument("--sort", default="frontier", choices=["frontier", "two_pass"],
+                    help="tile sort of the deposit: one pass with per-tile cursors, or two "
+                         "staged partition passes")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16,
@@ -63,7 +66,7 @@ def workload(a):
         "workload": "%d^3 grid, %d %s particles, %s deposit + %s window, axis %d, "
                     "BoxSize %g" % (a.dims, a.particles, a.positions, a.mas, a.mas, a.axis, BOX),
         "dims": a.dims, "particles": a.particles, "positions": a.positions,
-        "mas": a.mas, "axis": a.axis, "box": BOX,
+        "mas": a.mas, "axis": a.axis, "box": BOX, "sort": a.sort,
         "l2": "inputs larger than L2 (positions %.2f GB, grid %.2f GB) -- no flush"
               % (a.particles * 12 / 1e9, 4 * a.dims ** 3 / 1e9),
     }
@@ -264,10 +267,12 @@ def run_ours(a):
     mas = _native.MAS_CODE[a.mas]
     win = MAS_function(a.mas)
 
+    flags = _native.PYL_DEVICE_PTRS | (_native.PYL_SORT_TWO_PASS if a.sort == "two_pass" else 0)
+
     def step():
         rc = ctx.lib.pyl_pk_particles(ctx.ptr, ctypes.c_void_p(pos.data_ptr()), a.particles,
                                       None, a.dims, ctypes.c_float(BOX), mas, a.axis, win, 0,
-                                      ctypes.byref(out.struct), _native.PYL_DEVICE_PTRS)
+                                      ctypes.byref(out.struct), flags)
         ctx.check(rc)
 
     for _ in range(a.warmup):

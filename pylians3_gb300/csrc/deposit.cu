@@ -394,6 +394,40 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
     }
 }
 
+// Single-pass alternative to the two partition passes: every particle takes
+// the next slot of its tile with one atomic on the tile's global cursor
+// (lanes of a warp that share a tile take one atomic for all of them).
+// All writes of a tile happen at its advancing frontier, so the partially
+// written sectors stay in L2 until they are complete.
+template <int MAS, bool HAS_W>
+__global__ void __launch_bounds__(256)
+k_scatter_frontier(const float *__restrict__ src, const float *__restrict__ srcw, long long n,
+                   float inv, TileGeom g, unsigned *__restrict__ cursor,
+                   float *__restrict__ dst, float *__restrict__ dstw) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (long long b = (long long)blockIdx.x * blockDim.x; b < n;
+         b += (long long)gridDim.x * blockDim.x) {
+        const long long i = b + threadIdx.x;
+        const bool active = i < n;
+        const unsigned live = __ballot_sync(0xffffffffu, active);
+        if (!active) continue;
+        const float x = __ldcs(src + 3 * i), y = __ldcs(src + 3 * i + 1),
+                    z = __ldcs(src + 3 * i + 2);
+        const int t = tile_of<MAS>(x, y, z, inv, g);
+        const unsigned peers = __match_any_sync(live, t);
+        const int leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&cursor[t], (unsigned)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        const size_t slot = (size_t)base + __popc(peers & lt);
+        dst[3 * slot] = x;
+        dst[3 * slot + 1] = y;
+        dst[3 * slot + 2] = z;
+        if (HAS_W) dstw[slot] = __ldcs(srcw + i);
+    }
+}
+
 __device__ __forceinline__ void red_v4(float *addr, float a, float b, float c, float d) {
     asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
                  :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
@@ -565,7 +599,7 @@ size_t partition_smem(bool weighted) {
 
 template <int MAS, bool HAS_W>
 int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
-                    int dims, float inv, const TileGeom &g) {
+                    int dims, float inv, const TileGeom &g, bool two_pass) {
     int st = PYL_OK;
     const int nt = g.ntiles;
     // device scratch: counts/starts (nt+1), cursors, item bookkeeping
@@ -582,14 +616,18 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
     if (!items) return st;
     unsigned *nitems = (unsigned *)ws_get(ctx, "dep_nitems", sizeof(unsigned), &st);
     if (!nitems) return st;
-    float *b1 = (float *)ws_get(ctx, "dep_b1", sizeof(float) * 3 * (size_t)n, &st);
-    if (!b1) return st;
+    float *b1 = nullptr, *w1 = nullptr, *w2 = nullptr;
+    if (two_pass) {
+        b1 = (float *)ws_get(ctx, "dep_b1", sizeof(float) * 3 * (size_t)n, &st);
+        if (!b1) return st;
+    }
     float *b2 = (float *)ws_get(ctx, "dep_b2", sizeof(float) * 3 * (size_t)n, &st);
     if (!b2) return st;
-    float *w1 = nullptr, *w2 = nullptr;
     if (HAS_W) {
-        w1 = (float *)ws_get(ctx, "dep_w1", sizeof(float) * (size_t)n, &st);
-        if (!w1) return st;
+        if (two_pass) {
+            w1 = (float *)ws_get(ctx, "dep_w1", sizeof(float) * (size_t)n, &st);
+            if (!w1) return st;
+        }
         w2 = (float *)ws_get(ctx, "dep_w2", sizeof(float) * (size_t)n, &st);
         if (!w2) return st;
     }
@@ -614,18 +652,27 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         k_items<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(nchunk, start, nt, items, nitems);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
-        const size_t psm = partition_smem(HAS_W);
-        const long long nblk = (n + KP - 1) / KP;
-        if ((st = set_smem(ctx, k_partition<MAS, HAS_W, false>, psm))) return st;
-        k_partition<MAS, HAS_W, false><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
-            pos, W, b1, w1, n, inv, g, ccur, start);
-        ctx->launches++;
-        PYL_CUDA(ctx, cudaGetLastError());
-        if ((st = set_smem(ctx, k_partition<MAS, HAS_W, true>, psm))) return st;
-        k_partition<MAS, HAS_W, true><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
-            b1, w1, b2, w2, n, inv, g, fcur, start);
-        ctx->launches++;
-        PYL_CUDA(ctx, cudaGetLastError());
+        if (two_pass) {
+            const size_t psm = partition_smem(HAS_W);
+            const long long nblk = (n + KP - 1) / KP;
+            if ((st = set_smem(ctx, k_partition<MAS, HAS_W, false>, psm))) return st;
+            k_partition<MAS, HAS_W, false><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
+                pos, W, b1, w1, n, inv, g, ccur, start);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+            if ((st = set_smem(ctx, k_partition<MAS, HAS_W, true>, psm))) return st;
+            k_partition<MAS, HAS_W, true><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
+                b1, w1, b2, w2, n, inv, g, fcur, start);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+        } else {
+            long long blocks = (n + 255) / 256;
+            if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+            k_scatter_frontier<MAS, HAS_W><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
+                pos, W, n, inv, g, fcur, b2, w2);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+        }
     }
     const int vec4 = (dims % 4 == 0 && ((uintptr_t)grid & 15) == 0) ? 1 : 0;
     const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
@@ -644,10 +691,11 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
 
 template <int MAS>
 int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
-                  int dims, float inv) {
+                  int dims, float inv, int flags) {
     const TileGeom g = make_geom(dims, MAS);
-    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g)
-             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g);
+    const bool two_pass = (flags & PYL_SORT_TWO_PASS) != 0;
+    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, two_pass)
+             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, two_pass);
 }
 
 bool use_sorted(long long n, int coord, int dims, int mas, int flags) {
@@ -673,10 +721,10 @@ static int deposit_t(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const
     if (sizeof(G) == sizeof(float) && use_sorted(n, coord, dims, mas, flags)) {
         float *gf = reinterpret_cast<float *>(grid);
         switch (mas) {
-            case PYL_MAS_NGP: return launch_sorted<PYL_MAS_NGP>(ctx, pos, n, W, gf, dims, inv);
-            case PYL_MAS_CIC: return launch_sorted<PYL_MAS_CIC>(ctx, pos, n, W, gf, dims, inv);
-            case PYL_MAS_TSC: return launch_sorted<PYL_MAS_TSC>(ctx, pos, n, W, gf, dims, inv);
-            case PYL_MAS_PCS: return launch_sorted<PYL_MAS_PCS>(ctx, pos, n, W, gf, dims, inv);
+            case PYL_MAS_NGP: return launch_sorted<PYL_MAS_NGP>(ctx, pos, n, W, gf, dims, inv, flags);
+            case PYL_MAS_CIC: return launch_sorted<PYL_MAS_CIC>(ctx, pos, n, W, gf, dims, inv, flags);
+            case PYL_MAS_TSC: return launch_sorted<PYL_MAS_TSC>(ctx, pos, n, W, gf, dims, inv, flags);
+            case PYL_MAS_PCS: return launch_sorted<PYL_MAS_PCS>(ctx, pos, n, W, gf, dims, inv, flags);
             default: break;
         }
     }

@@ -133,7 +133,7 @@ k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
 
 // Fused x transform + binning over items (kyy, kz block), persistent CTAs.
 template <int N, int WHAT>
-__global__ void __launch_bounds__(ColsCfg<N>::THREADS, 1)
+__global__ void __launch_bounds__(ColsCfg<N>::THREADS, 2)
 k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restrict__ g_tw,
           const float *__restrict__ g_win, int axis, int kmax, PkAcc acc, int nitems,
           int fold_every) {
