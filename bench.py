@@ -51,9 +51,10 @@ def parse():
     ap.add_argument("--mas", default="CIC")
     ap.add_argument("--axis", type=int, default=0)
     ap.add_argument("--positions", default="uniform", choices=["uniform", "zeldovich"])
-    ap.add_argument("--sort", default="frontier", choices=["frontier", "two_pass"],
-                    help="tile sort of the deposit: one pass with per-tile cursors, or two "
-                         "staged partition passes")
+    ap.add_argument("--sort", default="auto", choices=["auto", "frontier", "two_pass"],
+                    help="tile sort of the deposit: chosen on the device from the input "
+                         "order (auto), one pass with per-tile cursors, or two staged "
+                         "partition passes")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16,
@@ -267,7 +268,8 @@ def run_ours(a):
     mas = _native.MAS_CODE[a.mas]
     win = MAS_function(a.mas)
 
-    flags = _native.PYL_DEVICE_PTRS | (_native.PYL_SORT_TWO_PASS if a.sort == "two_pass" else 0)
+    flags = _native.PYL_DEVICE_PTRS | {"auto": 0, "frontier": _native.PYL_SORT_FRONTIER,
+                                       "two_pass": _native.PYL_SORT_TWO_PASS}[a.sort]
 
     def step():
         rc = ctx.lib.pyl_pk_particles(ctx.ptr, ctypes.c_void_p(pos.data_ptr()), a.particles,

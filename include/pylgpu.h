@@ -52,8 +52,11 @@ enum { PYL_MAS_NONE = 0, PYL_MAS_NGP = 1, PYL_MAS_CIC = 2, PYL_MAS_TSC = 3,
 #define PYL_COMPENSATED  0x02  /* deposit: two-sum compensated accumulation    */
 #define PYL_DEPOSIT_ATOMIC 0x04 /* deposit: force the unsorted global-atomic path */
 #define PYL_DEPOSIT_SORTED 0x08 /* deposit: force the tile-sorted shared path  */
-#define PYL_SORT_TWO_PASS  0x10 /* tile sort: two staged partition passes instead
-                                   of one pass with per-tile global cursors   */
+/* The tile sort picks, on the device, one pass with per-tile global cursors
+ * for spatially coherent input order, two staged partition passes
+ * otherwise; these flags force one of them.                                */
+#define PYL_SORT_TWO_PASS  0x10
+#define PYL_SORT_FRONTIER  0x20
 
 /* Which Pk outputs to compute (bit mask); the 3D multipoles always are.   */
 #define PYL_PK_3D     0x00

@@ -252,28 +252,60 @@ __device__ __forceinline__ int tile_of(float x, float y, float z, float inv, con
 }
 
 // Counting pass: particles per tile (shared histogram, then global adds).
+// It also counts, over all warps, the distinct tiles among each warp's 32
+// consecutive particles: few distinct tiles mean the input order is already
+// spatially coherent (e.g. a displaced lattice), and the single-pass
+// frontier scatter is then the cheaper sort.
 template <int MAS>
 __global__ void __launch_bounds__(1024, 1)
 k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
-             unsigned *__restrict__ count) {
+             unsigned *__restrict__ count, unsigned *__restrict__ distinct) {
     extern __shared__ unsigned s_cnt[];
+    __shared__ unsigned s_distinct;
     for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x) s_cnt[t] = 0u;
+    if (threadIdx.x == 0) s_distinct = 0u;
     __syncthreads();
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        atomicAdd(&s_cnt[tile_of<MAS>(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1),
-                                      __ldg(pos + 3 * i + 2), inv, g)], 1u);
+    const int lane = threadIdx.x & 31;
+    unsigned leaders = 0;
+    for (long long b = (long long)blockIdx.x * blockDim.x; b < n;
+         b += (long long)gridDim.x * blockDim.x) {
+        const long long i = b + threadIdx.x;
+        const bool active = i < n;
+        const unsigned live = __ballot_sync(0xffffffffu, active);
+        if (!active) continue;
+        const int t = tile_of<MAS>(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1),
+                                   __ldg(pos + 3 * i + 2), inv, g);
+        const unsigned peers = __match_any_sync(live, t);
+        if (lane == __ffs(peers) - 1) {
+            atomicAdd(&s_cnt[t], (unsigned)__popc(peers));
+            ++leaders;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) leaders += __shfl_down_sync(0xffffffffu, leaders, o);
+    if (lane == 0 && leaders) atomicAdd(&s_distinct, leaders);
     __syncthreads();
     for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
         if (s_cnt[t]) atomicAdd(&count[t], s_cnt[t]);
+    if (threadIdx.x == 0 && s_distinct) atomicAdd(distinct, s_distinct);
 }
 
 // After the scan (start[0..ntiles] exclusive, start[ntiles] = n): the key
 // cursors of both passes and the deposit work items (tile, chunk) of every
 // non-empty tile, chunk = kItemCap particles.  nchunk is scanned separately.
+// Sort mode: 0 = frontier scatter, 1 = two partition passes; forced >= 0
+// overrides the choice made from the distinct-tiles-per-warp count (frontier
+// when a warp's 32 particles span at most 8 tiles on average).
+constexpr int kSortFrontier = 0, kSortTwoPass = 1;
+
 __global__ void k_sort_setup(const unsigned *__restrict__ start, int ntiles, int F, int ncoarse,
                              unsigned *__restrict__ fine_cur, unsigned *__restrict__ coarse_cur,
-                             unsigned *__restrict__ nchunk) {
+                             unsigned *__restrict__ nchunk, long long n,
+                             const unsigned *__restrict__ distinct, int forced,
+                             unsigned *__restrict__ mode) {
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *mode = forced >= 0 ? (unsigned)forced
+                            : ((long long)*distinct * 4 <= n ? kSortFrontier : kSortTwoPass);
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
         fine_cur[t] = start[t];
         const unsigned cnt = start[t + 1] - start[t];
@@ -300,7 +332,9 @@ template <int MAS, bool HAS_W, bool FINE>
 __global__ void __launch_bounds__(kPartThreads, 4)
 k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             float *__restrict__ dst, float *__restrict__ dstw, long long n, float inv,
-            TileGeom g, unsigned *__restrict__ cursor, const unsigned *__restrict__ start) {
+            TileGeom g, unsigned *__restrict__ cursor, const unsigned *__restrict__ start,
+            const unsigned *__restrict__ mode) {
+    if (*mode != kSortTwoPass) return;   // the whole grid takes the same branch
     extern __shared__ float sm[];
     float *sp = sm;                    // 3*KP staged particles (input order)
     float *sp2 = sp + 3 * KP;          // 3*KP particles in key order
@@ -403,7 +437,9 @@ template <int MAS, bool HAS_W>
 __global__ void __launch_bounds__(256)
 k_scatter_frontier(const float *__restrict__ src, const float *__restrict__ srcw, long long n,
                    float inv, TileGeom g, unsigned *__restrict__ cursor,
-                   float *__restrict__ dst, float *__restrict__ dstw) {
+                   float *__restrict__ dst, float *__restrict__ dstw,
+                   const unsigned *__restrict__ mode) {
+    if (*mode != kSortFrontier) return;   // the whole grid takes the same branch
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     for (long long b = (long long)blockIdx.x * blockDim.x; b < n;
@@ -599,12 +635,16 @@ size_t partition_smem(bool weighted) {
 
 template <int MAS, bool HAS_W>
 int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
-                    int dims, float inv, const TileGeom &g, bool two_pass) {
+                    int dims, float inv, const TileGeom &g, int forced_mode) {
     int st = PYL_OK;
     const int nt = g.ntiles;
+    const bool two_pass = forced_mode != kSortFrontier;   // may be chosen on the device
     // device scratch: counts/starts (nt+1), cursors, item bookkeeping
     unsigned *start = (unsigned *)ws_get(ctx, "dep_start", sizeof(unsigned) * (size_t)(nt + 1), &st);
     if (!start) return st;
+    unsigned *flags2 = (unsigned *)ws_get(ctx, "dep_mode", 2 * sizeof(unsigned), &st);
+    if (!flags2) return st;
+    unsigned *distinct = flags2, *mode = flags2 + 1;
     unsigned *fcur = (unsigned *)ws_get(ctx, "dep_fcur", sizeof(unsigned) * (size_t)nt, &st);
     if (!fcur) return st;
     unsigned *ccur = (unsigned *)ws_get(ctx, "dep_ccur", sizeof(unsigned) * (size_t)g.ncoarse, &st);
@@ -636,15 +676,17 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
     {
         StageScope s(ctx, ST_SORT);
         PYL_CUDA(ctx, cudaMemsetAsync(start, 0, sizeof(unsigned) * (size_t)(nt + 1), ctx->stream));
+        PYL_CUDA(ctx, cudaMemsetAsync(flags2, 0, 2 * sizeof(unsigned), ctx->stream));
         const size_t hsm = sizeof(unsigned) * (size_t)nt;
         if ((st = set_smem(ctx, k_tile_count<MAS>, hsm))) return st;
-        k_tile_count<MAS><<<sms, 1024, hsm, ctx->stream>>>(pos, n, inv, g, start);
+        k_tile_count<MAS><<<sms, 1024, hsm, ctx->stream>>>(pos, n, inv, g, start, distinct);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         // exclusive scan over nt+1 entries (the extra 0 becomes the total n)
         if ((st = scan_exclusive(ctx, start, nt + 1))) return st;
         k_sort_setup<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(start, nt, g.F, g.ncoarse, fcur,
-                                                                ccur, nchunk);
+                                                                ccur, nchunk, n, distinct,
+                                                                forced_mode, mode);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         PYL_CUDA(ctx, cudaMemsetAsync(nchunk + nt, 0, sizeof(unsigned), ctx->stream));
@@ -652,24 +694,27 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         k_items<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(nchunk, start, nt, items, nitems);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
+        // Both sorts are enqueued unless one is forced; each kernel reads the
+        // mode chosen on the device and the other one returns at once.
         if (two_pass) {
             const size_t psm = partition_smem(HAS_W);
             const long long nblk = (n + KP - 1) / KP;
             if ((st = set_smem(ctx, k_partition<MAS, HAS_W, false>, psm))) return st;
             k_partition<MAS, HAS_W, false><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
-                pos, W, b1, w1, n, inv, g, ccur, start);
+                pos, W, b1, w1, n, inv, g, ccur, start, mode);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
             if ((st = set_smem(ctx, k_partition<MAS, HAS_W, true>, psm))) return st;
             k_partition<MAS, HAS_W, true><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
-                b1, w1, b2, w2, n, inv, g, fcur, start);
+                b1, w1, b2, w2, n, inv, g, fcur, start, mode);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
-        } else {
+        }
+        if (forced_mode != kSortTwoPass) {
             long long blocks = (n + 255) / 256;
             if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
             k_scatter_frontier<MAS, HAS_W><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
-                pos, W, n, inv, g, fcur, b2, w2);
+                pos, W, n, inv, g, fcur, b2, w2, mode);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
         }
@@ -693,9 +738,10 @@ template <int MAS>
 int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
                   int dims, float inv, int flags) {
     const TileGeom g = make_geom(dims, MAS);
-    const bool two_pass = (flags & PYL_SORT_TWO_PASS) != 0;
-    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, two_pass)
-             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, two_pass);
+    const int forced = (flags & PYL_SORT_TWO_PASS) ? kSortTwoPass
+                       : (flags & PYL_SORT_FRONTIER) ? kSortFrontier : -1;
+    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced)
+             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced);
 }
 
 bool use_sorted(long long n, int coord, int dims, int mas, int flags) {

@@ -60,6 +60,7 @@ def test_paths_match_oracle(native, oracle, dims, MAS, kind):
         tol = 1e-5 * max(1.0, float(np.abs(ref).max()))
         for flags in (native.PYL_DEPOSIT_SORTED,
                       native.PYL_DEPOSIT_SORTED | native.PYL_SORT_TWO_PASS,
+                      native.PYL_DEPOSIT_SORTED | native.PYL_SORT_FRONTIER,
                       native.PYL_DEPOSIT_ATOMIC):
             g = run_ma(native, pos, dims, MAS, w, flags)
             assert float(np.abs(g - ref).max()) <= tol, (flags, w is None)
