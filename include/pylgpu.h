@@ -166,6 +166,24 @@ int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n,
                      int axis, int mas_window, int what, pyl_pk_out *out,
                      int flags);
 
+/* Power spectrum of a device grid without allocating device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- a host application whose pool allocator owns the whole
+ * device, a plugin host that forbids allocations outside its allocator, or
+ * a latency-critical loop where cudaMalloc/cudaFree would synchronise the
+ * device.  Same arguments and outputs as pyl_pk, except: delta must be a
+ * device pointer; dims must be a power of two in [16, 128], other sizes
+ * return PYL_ERR_UNSUPPORTED.  All intermediates live in one fixed 12 MiB
+ * array of device memory inside the library, which every GPU that loads the
+ * library holds until the process exits.  The first call on a device looks
+ * up that array's address (make it before any stream capture).  Calls share
+ * the array and it keeps the last call's contents (the sums are cleared on
+ * every call); calls that overlap on the GPU race, so issue them one after
+ * another.  Nothing is allocated on the device, by this call or the context
+ * (create the context with a caller stream so that it makes no stream).    */
+int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double BoxSize,
+                   int axis, int mas, int what, pyl_pk_out *out);
+
 #ifdef __cplusplus
 }
 #endif

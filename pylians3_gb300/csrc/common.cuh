@@ -182,4 +182,26 @@ int mode_counts(pyl_ctx *ctx, int dims, int axis, unsigned long long *cnt_n,
 
 inline int isqrt_host(long long v) { return (int)__builtin_sqrt((double)v); }
 
+// ------------------------------------------------- spectrum bookkeeping (ctx.cu)
+// Device layout of the float64 sums of one Pk evaluation, followed by the raw
+// k = 0 mode (float2), the deposited mass (double) and the FFT shift (float).
+struct AccLayout {
+    size_t n3, n1, nph, n2;
+    size_t bytes() const { return sizeof(double) * (n3 + n1 + nph + n2) + 64; }
+};
+AccLayout acc_layout(const ModeTables &T);
+PkAcc acc_view(void *base, const AccLayout &L);
+// Finalisation of class Pk from the raw sums (host, float64).
+int finalize(pyl_ctx *ctx, const ModeTables &T, const std::vector<double> &raw,
+             const AccLayout &L, double BoxSize, int what, double inv_mean2, bool zero_dc2d,
+             pyl_pk_out *out);
+int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double> &raw,
+                 float2 *dc, double *mass);
+void twiddles_host(int n, std::vector<float2> &tw);
+void window_host(int dims, int mas, std::vector<float> &w);
+// Mode tables: sizes of the count arrays, and the tables from the counts.
+void mode_table_init(ModeTables &T, int dims, int axis, size_t &nn, size_t &n1, size_t &n2);
+void mode_table_fill(ModeTables &T, const unsigned long long *h, size_t nn, size_t n1,
+                     size_t n2);
+
 }  // namespace pyl

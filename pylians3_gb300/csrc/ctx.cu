@@ -83,6 +83,29 @@ int stage_flush(pyl_ctx *ctx) {
     return PYL_OK;
 }
 
+// tw[m] = exp(-2 pi i m / n), evaluated in double and rounded to float
+void twiddles_host(int n, std::vector<float2> &tw) {
+    tw.resize(n);
+    for (int m = 0; m < n; ++m) {
+        const double a = 2.0 * M_PI * (double)m / (double)n;
+        tw[m] = make_float2((float)cos(a), (float)(-sin(a)));
+    }
+}
+
+// MAS_correction (Pk_library.pyx:83-84) per grid index: 1 if x == 0 else
+// (x / sin x)^p, x = pi * k / dims with k the signed frequency of index i.
+void window_host(int dims, int mas, std::vector<float> &w) {
+    if (mas < 1 || mas > 4) mas = 0;
+    const int middle = dims / 2;
+    w.resize(dims);
+    const double prefact = M_PI / dims;
+    for (int i = 0; i < dims; ++i) {
+        const int k = i > middle ? i - dims : i;
+        const double x = prefact * k;
+        w[i] = (float)((x == 0.0) ? 1.0 : pow(x / sin(x), mas));
+    }
+}
+
 static void factorize(int n, FftDesc &D) {
     D.n = n;
     D.nst = 0;
@@ -104,11 +127,8 @@ const FftPlan *fft_plan(pyl_ctx *ctx, int n, int *status) {
     if (it != ctx->fft.end()) return &it->second;
     FftPlan P;
     factorize(n, P.desc);
-    std::vector<float2> tw(n);
-    for (int m = 0; m < n; ++m) {
-        const double a = 2.0 * M_PI * (double)m / (double)n;
-        tw[m] = make_float2((float)cos(a), (float)(-sin(a)));
-    }
+    std::vector<float2> tw;
+    twiddles_host(n, tw);
     cudaError_t e = cudaMalloc(&P.d_tw, sizeof(float2) * n);
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle table"); return nullptr; }
     e = cudaMemcpy(P.d_tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
@@ -123,14 +143,8 @@ const float *window_table(pyl_ctx *ctx, int dims, int mas, int *status) {
     auto key = std::make_pair(dims, mas);
     auto it = ctx->win.find(key);
     if (it != ctx->win.end()) return it->second;
-    const int middle = dims / 2;
-    std::vector<float> w(dims);
-    const double prefact = M_PI / dims;
-    for (int i = 0; i < dims; ++i) {
-        const int k = i > middle ? i - dims : i;
-        const double x = prefact * k;
-        w[i] = (float)((x == 0.0) ? 1.0 : pow(x / sin(x), mas));
-    }
+    std::vector<float> w;
+    window_host(dims, mas, w);
     float *d = nullptr;
     cudaError_t e = cudaMalloc(&d, sizeof(float) * dims);
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "window table"); return nullptr; }
@@ -147,36 +161,23 @@ static void sizes(int dims, int &kmax, int &kmax_par, int &kmax_per) {
     kmax = isqrt_host(3 * middle * middle);
 }
 
-const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status) {
-    if (axis != 0 && axis != 1) axis = 2;
-    auto key = std::make_pair(dims, axis);
-    auto it = ctx->modes.find(key);
-    if (it != ctx->modes.end()) return &it->second;
-    ModeTables T;
+void mode_table_init(ModeTables &T, int dims, int axis, size_t &nn, size_t &n1, size_t &n2) {
+    T = ModeTables();
     T.dims = dims;
-    T.axis = axis;
+    T.axis = (axis != 0 && axis != 1) ? 2 : axis;
     sizes(dims, T.kmax, T.kmax_par, T.kmax_per);
     const long long middle = dims / 2;
-    const size_t nn = (size_t)(3 * middle * middle + 1);
-    const size_t n1 = (size_t)(middle + 1);
-    const size_t n2 = (size_t)(middle + 1) * (T.kmax_per + 1);
-    int st = PYL_OK;
-    unsigned long long *d = (unsigned long long *)ws_get(
-        ctx, "mode_counts", sizeof(unsigned long long) * (nn + n1 + n2), &st);
-    if (!d) { *status = st; return nullptr; }
-    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * (nn + n1 + n2), ctx->stream);
-    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count memset"); return nullptr; }
-    if ((st = mode_counts(ctx, dims, axis, d, d + nn, d + nn + n1, T.kmax_per))) {
-        *status = st;
-        return nullptr;
-    }
-    std::vector<unsigned long long> h(nn + n1 + n2);
-    e = cudaMemcpyAsync(h.data(), d, sizeof(unsigned long long) * h.size(),
-                        cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count download"); return nullptr; }
+    nn = (size_t)(3 * middle * middle + 1);
+    n1 = (size_t)(middle + 1);
+    n2 = (size_t)(middle + 1) * (T.kmax_per + 1);
+}
+
+// Per-bin tables from the integer counts (counts per k^2, 1D, 2D).
+void mode_table_fill(ModeTables &T, const unsigned long long *h, size_t nn, size_t n1,
+                     size_t n2) {
     T.N3D.assign(T.kmax + 1, 0.0);
     T.k3Dsum.assign(T.kmax + 1, 0.0);
+    T.total = 0;
     for (size_t v = 0; v < nn; ++v) {
         if (!h[v]) continue;
         const int b = isqrt_host((long long)v);
@@ -192,6 +193,32 @@ const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status) {
     }
     T.N2D.resize(n2);
     for (size_t i = 0; i < n2; ++i) T.N2D[i] = (double)h[nn + n1 + i];
+}
+
+const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status) {
+    if (axis != 0 && axis != 1) axis = 2;
+    auto key = std::make_pair(dims, axis);
+    auto it = ctx->modes.find(key);
+    if (it != ctx->modes.end()) return &it->second;
+    ModeTables T;
+    size_t nn, n1, n2;
+    mode_table_init(T, dims, axis, nn, n1, n2);
+    int st = PYL_OK;
+    unsigned long long *d = (unsigned long long *)ws_get(
+        ctx, "mode_counts", sizeof(unsigned long long) * (nn + n1 + n2), &st);
+    if (!d) { *status = st; return nullptr; }
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * (nn + n1 + n2), ctx->stream);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count memset"); return nullptr; }
+    if ((st = mode_counts(ctx, dims, axis, d, d + nn, d + nn + n1, T.kmax_per))) {
+        *status = st;
+        return nullptr;
+    }
+    std::vector<unsigned long long> h(nn + n1 + n2);
+    e = cudaMemcpyAsync(h.data(), d, sizeof(unsigned long long) * h.size(),
+                        cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count download"); return nullptr; }
+    mode_table_fill(T, h.data(), nn, n1, n2);
     return &(ctx->modes[key] = T);
 }
 
@@ -467,12 +494,7 @@ int pyl_fft_c2r(pyl_ctx *ctx, const float *in, float *out, int dims, int flags) 
 }  // extern "C"
 
 // ---------------------------------------------------------------------- Pk
-namespace {
-
-struct AccLayout {
-    size_t n3, n1, nph, n2;
-    size_t bytes() const { return sizeof(double) * (n3 + n1 + nph + n2) + 64; }
-};
+namespace pyl {
 
 AccLayout acc_layout(const ModeTables &T) {
     AccLayout L;
@@ -623,7 +645,7 @@ int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double
     return PYL_OK;
 }
 
-}  // namespace
+}  // namespace pyl
 
 extern "C" {
 
