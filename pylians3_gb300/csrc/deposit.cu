@@ -252,10 +252,11 @@ __device__ __forceinline__ int tile_of(float x, float y, float z, float inv, con
 }
 
 // Counting pass: particles per tile (shared histogram, then global adds).
-// It also counts, over all warps, the distinct tiles among each warp's 32
-// consecutive particles: few distinct tiles mean the input order is already
-// spatially coherent (e.g. a displaced lattice), and the single-pass
-// frontier scatter is then the cheaper sort.
+// It also counts tile changes between neighbouring particles of each warp
+// (particle i vs i-1): few changes mean the input order is already spatially
+// coherent (e.g. a displaced lattice), and the single-pass frontier scatter
+// is then the cheaper sort.  A warp whose 32 particles share one tile adds
+// them with one shared atomic.
 template <int MAS>
 __global__ void __launch_bounds__(1024, 1)
 k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
@@ -266,24 +267,28 @@ k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
     if (threadIdx.x == 0) s_distinct = 0u;
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    unsigned leaders = 0;
+    unsigned changes = 0;
     for (long long b = (long long)blockIdx.x * blockDim.x; b < n;
          b += (long long)gridDim.x * blockDim.x) {
         const long long i = b + threadIdx.x;
         const bool active = i < n;
-        const unsigned live = __ballot_sync(0xffffffffu, active);
-        if (!active) continue;
-        const int t = tile_of<MAS>(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1),
-                                   __ldg(pos + 3 * i + 2), inv, g);
-        const unsigned peers = __match_any_sync(live, t);
-        if (lane == __ffs(peers) - 1) {
-            atomicAdd(&s_cnt[t], (unsigned)__popc(peers));
-            ++leaders;
+        const int t = active ? tile_of<MAS>(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1),
+                                            __ldg(pos + 3 * i + 2), inv, g)
+                             : -1;
+        const int prev = __shfl_up_sync(0xffffffffu, t, 1);
+        const int first = __shfl_sync(0xffffffffu, t, 0);
+        const bool same = __all_sync(0xffffffffu, t == first);
+        if (same) {
+            if (lane == 0 && t >= 0) atomicAdd(&s_cnt[t], 32u);
+            changes += (lane == 0) ? 1u : 0u;
+        } else if (active) {
+            atomicAdd(&s_cnt[t], 1u);
+            changes += (lane == 0 || t != prev) ? 1u : 0u;
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) leaders += __shfl_down_sync(0xffffffffu, leaders, o);
-    if (lane == 0 && leaders) atomicAdd(&s_distinct, leaders);
+    for (int o = 16; o > 0; o >>= 1) changes += __shfl_down_sync(0xffffffffu, changes, o);
+    if (lane == 0 && changes) atomicAdd(&s_distinct, changes);
     __syncthreads();
     for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
         if (s_cnt[t]) atomicAdd(&count[t], s_cnt[t]);

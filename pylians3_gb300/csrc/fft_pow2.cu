@@ -131,12 +131,13 @@ k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
     }
 }
 
-// Fused x transform + binning over items (kyy, kz block), persistent CTAs.
+// Fused x transform + binning.  A CTA bins `ipb` consecutive work items
+// (kyy, kz block) into float32 shared histograms (a few hundred terms per bin
+// at most) and adds them to the float64 sums when it ends.
 template <int N, int WHAT>
-__global__ void __launch_bounds__(ColsCfg<N>::THREADS, 2)
+__global__ void __launch_bounds__(ColsCfg<N>::THREADS, (ColsCfg<N>::THREADS >= 512 ? 2 : 4))
 k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restrict__ g_tw,
-          const float *__restrict__ g_win, int axis, int kmax, PkAcc acc, int nitems,
-          int fold_every) {
+          const float *__restrict__ g_win, int axis, int kmax, PkAcc acc, int nitems, int ipb) {
     using CF = ColsCfg<N>;
     constexpr int P = CF::P, C = CF::C, LINE = Pow2<N>::LINE;
     constexpr int MID = N / 2;
@@ -145,13 +146,14 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
     const int c = threadIdx.x % C, t = threadIdx.x / C;
     float2 *line = sm + N + c * LINE;
     float *win = reinterpret_cast<float *>(sm + N + C * LINE);
-    BinHist H;
+    FltHist H;
     H.setup(win + N, kmax, MID, WHAT);
     for (int i = threadIdx.x; i < N; i += blockDim.x) { tw[i] = g_tw[i]; win[i] = g_win[i]; }
     H.zero_all();
     __syncthreads();
     const int nzb = (h + C - 1) / C;
-    int since_fold = 0;
+    const int it0 = blockIdx.x * ipb;
+    const int it1 = min(nitems, it0 + ipb);
     // column c of item `item`, element s of thread t -> registers
     auto load = [&](int item, float2 (&v)[8]) {
         const int kz = (item % nzb) * C + c;
@@ -163,8 +165,8 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
             v[s] = valid ? __ldcs(base + (int64_t)(t + s * P) * es) : make_float2(0.f, 0.f);
     };
     float2 v[8];
-    if (blockIdx.x < nitems) load(blockIdx.x, v);
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    if (it0 < it1) load(it0, v);
+    for (int it = it0; it < it1; ++it) {
         const int kyy = it / nzb;
         fft_line<N, -1>(v, t, line, tw);
         // natural order into the line, then each thread bins a run of 8
@@ -173,7 +175,7 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
         for (int u = 0; u < 8; ++u) line[pad8(t + u * P)] = v[u];
         __syncthreads();
         // the next item's loads are in flight while this one is binned
-        if (it + (int)gridDim.x < nitems) load(it + gridDim.x, v);
+        if (it + 1 < it1) load(it + 1, v);
         {
             const int cc = threadIdx.x / P, rr = threadIdx.x % P;
             const int kzc = (it % nzb) * C + cc;
@@ -191,17 +193,9 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
                 R.flush(H);
             }
         }
-        if (++since_fold == fold_every) {
-            since_fold = 0;
-            __syncthreads();
-            H.fold();
-        }
         __syncthreads();   // the shared lines are reused by the next item
     }
-    __syncthreads();
-    H.fold();
-    __syncthreads();
-    H.flush(acc, MID, WHAT);
+    H.flush(acc);
 }
 
 template <typename K>
@@ -268,20 +262,19 @@ int pk_n(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const float2
          const float *win, int kmax, const PkAcc &acc) {
     using CF = ColsCfg<N>;
     const size_t smem = sizeof(float2) * (N + (size_t)CF::C * Pow2<N>::LINE) +
-                        sizeof(float) * N + BinHist::bytes(kmax, N / 2, WHAT);
+                        sizeof(float) * N + FltHist::bytes(kmax, N / 2, WHAT);
     if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "Pk histogram too large");
     int st;
     if ((st = set_smem(ctx, k_pk_x_p2<N, WHAT>, smem))) return st;
-    int per_sm = 0;
-    PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pk_x_p2<N, WHAT>,
-                                                               CF::THREADS, smem));
-    int sms = 0;
-    PYL_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    // items per CTA: enough CTAs to fill the GPU several times over, few
+    // enough that the per-CTA float64 flush stays small
     const int nitems = N * ((h + CF::C - 1) / CF::C);
-    int grid = (per_sm > 0 ? per_sm : 1) * sms;
-    if (grid > nitems) grid = nitems;
+    int ipb = nitems / (152 * 16);
+    if (ipb < 1) ipb = 1;
+    if (ipb > 8) ipb = 8;
+    const int grid = (nitems + ipb - 1) / ipb;
     k_pk_x_p2<N, WHAT><<<grid, CF::THREADS, smem, ctx->stream>>>(data, h, rs, tw, win, axis, kmax,
-                                                                 acc, nitems, 4);
+                                                                 acc, nitems, ipb);
     ctx->launches++;
     PYL_CUDA(ctx, cudaGetLastError());
     return PYL_OK;

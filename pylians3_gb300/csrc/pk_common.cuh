@@ -64,8 +64,8 @@ struct BinHist {
 
 // The extra (non-3D) outputs of one mode: 1D and phase into the shared
 // histograms, 2D into the global float64 sums.
-template <int WHAT>
-__device__ __forceinline__ void mode_extras(BinHist &H, const PkAcc &acc, int n2, int bin,
+template <int WHAT, class Hist>
+__device__ __forceinline__ void mode_extras(Hist &H, const PkAcc &acc, int n2, int bin,
                                             int kpar, float re, float d2, int mid) {
     if (WHAT & PYL_PK_1D) {
         if (n2 <= mid * mid) atomicAdd(&H.h1[abs(kpar)], d2);
@@ -86,7 +86,8 @@ __device__ __forceinline__ void mode_extras(BinHist &H, const PkAcc &acc, int n2
 struct BinRun {
     int bin = -1;
     float p0 = 0.f, p2 = 0.f, p4 = 0.f;
-    __device__ __forceinline__ void flush(BinHist &H) {
+    template <class Hist>
+    __device__ __forceinline__ void flush(Hist &H) {
         if (bin >= 0) {
             atomicAdd(&H.h3[3 * bin + 0], p0);
             atomicAdd(&H.h3[3 * bin + 1], p2);
@@ -95,7 +96,8 @@ struct BinRun {
         bin = -1;
         p0 = p2 = p4 = 0.f;
     }
-    __device__ __forceinline__ void add(BinHist &H, int b, float d2, float mu2) {
+    template <class Hist>
+    __device__ __forceinline__ void add(Hist &H, int b, float d2, float mu2) {
         if (b != bin) {
             flush(H);
             bin = b;
@@ -107,8 +109,8 @@ struct BinRun {
 };
 
 // Same per-mode work as bin_mode, accumulating the multipoles into a run.
-template <int WHAT>
-__device__ __forceinline__ void bin_mode_run(BinRun &R, BinHist &H, const PkAcc &acc, float2 v,
+template <int WHAT, class Hist>
+__device__ __forceinline__ void bin_mode_run(BinRun &R, Hist &H, const PkAcc &acc, float2 v,
                                              int kxx, int ky, int kz, int n, int axis, float wx,
                                              float wyz, int mid) {
     const bool even = (n & 1) == 0;
@@ -130,6 +132,36 @@ __device__ __forceinline__ void bin_mode_run(BinRun &R, BinHist &H, const PkAcc 
     R.add(H, bin, d2, mu2);
     if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
 }
+
+// Float32-only shared histograms of one CTA, added to the global float64
+// sums when the CTA ends (used where a CTA bins a bounded number of modes).
+struct FltHist {
+    float *h3, *h1, *hph;
+    int n3, n1, nph;
+    __host__ static size_t bytes(int kmax, int mid, int what) {
+        return sizeof(float) * (3 * (size_t)(kmax + 1) + BinHist::count1(mid, what) +
+                                BinHist::countph(kmax, what));
+    }
+    __device__ void setup(float *base, int kmax, int mid, int what) {
+        n3 = 3 * (kmax + 1);
+        n1 = BinHist::count1(mid, what);
+        nph = BinHist::countph(kmax, what);
+        h3 = base;
+        h1 = h3 + n3;
+        hph = h1 + n1;
+    }
+    __device__ void zero_all() {
+        for (int i = threadIdx.x; i < n3 + n1 + nph; i += blockDim.x) h3[i] = 0.f;
+    }
+    __device__ void flush(const PkAcc &acc) {
+        for (int i = threadIdx.x; i < n3; i += blockDim.x)
+            if (h3[i] != 0.f) atomicAdd(&acc.P3[i], (double)h3[i]);
+        for (int i = threadIdx.x; i < n1; i += blockDim.x)
+            if (h1[i] != 0.f) atomicAdd(&acc.P1[i], (double)h1[i]);
+        for (int i = threadIdx.x; i < nph; i += blockDim.x)
+            if (hph[i] != 0.f) atomicAdd(&acc.Pph[i], (double)hph[i]);
+    }
+};
 
 // One independent mode (kxx, ky, kz) with raw value v: Hermitian half-space
 // selection (:324-327), |k| bin = floor(sqrt(kx^2 + ky^2 + kz^2)) exactly,
