@@ -183,14 +183,8 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
                 const float2 *ln = sm + N + cc * LINE;
                 const int ky = kyy > MID ? kyy - N : kyy;
                 const float wyz = win[kyy] * win[kzc];
-                BinRun R;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int kxx = 8 * rr + i;
-                    bin_mode_run<WHAT>(R, H, acc, ln[pad8(kxx)], kxx, ky, kzc, N, axis,
-                                       win[kxx], wyz, MID);
-                }
-                R.flush(H);
+                bin_run8<WHAT>(H, acc, ln, [](int i) { return pad8(i); }, 8 * rr, ky, kzc, N,
+                               axis, win, wyz, MID);
             }
         }
         __syncthreads();   // the shared lines are reused by the next item

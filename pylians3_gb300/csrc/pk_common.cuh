@@ -133,6 +133,44 @@ __device__ __forceinline__ void bin_mode_run(BinRun &R, Hist &H, const PkAcc &ac
     if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
 }
 
+// Eight consecutive modes kxx0 .. kxx0+7 of one pencil (ky, kz fixed), read
+// from shared memory at ln[pad(kxx)]: the same work as bin_mode_run, with the
+// bin index updated incrementally (n2 changes by 2 kx + 1 between neighbours)
+// instead of one square root per mode.
+template <int WHAT, class Hist, class Pad>
+__device__ __forceinline__ void bin_run8(Hist &H, const PkAcc &acc, const float2 *ln, Pad pad,
+                                         int kxx0, int ky, int kz, int n, int axis,
+                                         const float *win, float wyz, int mid) {
+    const bool even = (n & 1) == 0;
+    const bool plane = (kz == 0 || (kz == mid && even));
+    const int r2 = ky * ky + kz * kz;
+    const int kx0 = kxx0 > mid ? kxx0 - n : kxx0;
+    int bin = isqrt_dev(kx0 * kx0 + r2);
+    BinRun R;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int kxx = kxx0 + i;
+        const int kx = kxx > mid ? kxx - n : kxx;
+        const int n2 = kx * kx + r2;
+        while (bin * bin > n2) --bin;
+        while ((bin + 1) * (bin + 1) <= n2) ++bin;
+        if (plane) {
+            if (kx < 0) continue;
+            if ((kx == 0 || (kx == mid && even)) && ky < 0) continue;
+        }
+        const float2 v = ln[pad(kxx)];
+        if (n2 == 0) *acc.dc = v;
+        const int kpar = axis == 0 ? kx : (axis == 1 ? ky : kz);
+        const float f = win[kxx] * wyz;
+        const float re = v.x * f, im = v.y * f;
+        const float d2 = re * re + im * im;
+        const float mu2 = n2 > 0 ? (float)(kpar * kpar) * __frcp_rn((float)n2) : 0.f;
+        R.add(H, bin, d2, mu2);
+        if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
+    }
+    R.flush(H);
+}
+
 // Float32-only shared histograms of one CTA, added to the global float64
 // sums when the CTA ends (used where a CTA bins a bounded number of modes).
 struct FltHist {
