@@ -46,6 +46,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="plain", choices=["plain", "batched", "served"],
+                    help="plain: the headline line; batched: 64 uneven realizations "
+                         "overlapped; served: Poisson request streams")
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--rates", type=float, nargs="*", default=[50.0, 200.0, 500.0])
+    ap.add_argument("--seconds", type=float, default=5.0)
     ap.add_argument("--dims", type=int, default=512)
     ap.add_argument("--particles", type=int, default=512 ** 3)
     ap.add_argument("--mas", default="CIC")
@@ -386,10 +392,130 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------ batched and served forms
+def batched_requests(torch, seed=4242, count=64):
+    """64 realizations of uneven size: dims in {128, 192, 256, 384},
+    particles log-uniform in [2^20, 2^25], uniform or Zel'dovich (sigma 2-5
+    Mpc/h) positions, optional lognormal(0, 0.5) weights, CIC or TSC."""
+    import numpy as np
+    from pylians3_gb300 import synth
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        dims = int(rng.choice([128, 192, 256, 384]))
+        n = int(2 ** rng.uniform(20, 25))
+        if rng.random() < 0.5:
+            pos = synth.uniform(n, BOX, seed=seed + i)
+        else:
+            side = max(2, int(round(n ** (1.0 / 3.0))))
+            pos = synth.zeldovich(side, BOX, sigma=float(rng.uniform(2, 5)), seed=seed + i)
+        W = None
+        if rng.random() < 0.5:
+            g = torch.Generator(device="cuda").manual_seed(seed + 1000 + i)
+            W = torch.exp(0.5 * torch.randn(pos.shape[0], generator=g, device="cuda"))
+        reqs.append(dict(pos=pos, dims=dims, BoxSize=BOX, W=W,
+                         MAS=str(rng.choice(["CIC", "TSC"])), axis=int(rng.integers(0, 3))))
+    torch.cuda.synchronize()
+    return reqs
+
+
+def run_batched(a):
+    import torch
+    import pylians3_gb300 as P
+    from pylians3_gb300.serving import run_batch
+    reqs = batched_requests(torch)
+    for r in reqs[:4]:
+        P.power_spectrum(**r)          # plans, mode tables
+    ctx = P.context(0)
+    for r in reqs:
+        P.power_spectrum(**r, ctx=ctx)  # warm every shape once
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        P.power_spectrum(**r, ctx=ctx)
+    t_seq = time.perf_counter() - t0
+    run_batch(reqs, slots=a.slots)                 # warm the slots
+    res, t_bat = run_batch(reqs, slots=a.slots)
+    line = {"mode": "batched", "metric": "realizations/s (64 uneven realizations)",
+            "value": len(reqs) / t_bat, "unit": "spectra/s",
+            "sequential_value": len(reqs) / t_seq, "speedup": t_seq / t_bat,
+            "slots": a.slots, "particles_total": int(sum(r["pos"].shape[0] for r in reqs)),
+            "config": {"dims": "U{128,192,256,384}", "particles": "2^U(20,25)",
+                       "positions": "uniform | zeldovich sigma U(2,5)", "W": "lognormal(0,0.5) half",
+                       "mas": "U{CIC,TSC}"}}
+    print(json.dumps(line), flush=True)
+
+
+def served_pool(torch, max_ppc=8):
+    """Device-resident particle pools, one per grid size, 8 particles/cell."""
+    from pylians3_gb300 import synth
+    return {d: synth.uniform(max_ppc * d ** 3, BOX, seed=77 + d) for d in (64, 128, 256, 512)}
+
+
+def run_served(a):
+    import numpy as np
+    import torch
+    import pylians3_gb300 as P
+    from pylians3_gb300.serving import Server
+    pool = served_pool(torch)
+    torch.cuda.synchronize()
+
+    def stream(rate, seconds, seed):
+        rng = np.random.default_rng(seed)
+        t, out = 0.0, []
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t > seconds:
+                return out
+            d = int(rng.choice([64, 128, 256, 512], p=[0.3, 0.3, 0.3, 0.1]))
+            n = int(rng.integers(1, 9)) * d ** 3
+            off = int(rng.integers(0, pool[d].shape[0] - n + 1))
+            out.append((t, dict(pos=pool[d][off:off + n], dims=d, BoxSize=BOX,
+                                MAS=str(rng.choice(["NGP", "CIC", "TSC", "PCS"])),
+                                axis=int(rng.integers(0, 3)))))
+
+    # warm the plans and mode tables of every (dims, axis)
+    for d in (64, 128, 256, 512):
+        for ax in range(3):
+            P.power_spectrum(pool[d][:d ** 3], d, BOX, "CIC", axis=ax)
+    results = []
+    for rate in a.rates:
+        reqs = stream(rate, a.seconds, seed=int(rate))
+        row = {"rate": rate, "requests": len(reqs)}
+        for name, slots in (("served", a.slots), ("queue_only", 1)):
+            srv = Server(slots=slots, hbm_budget=150e9)
+            t0 = time.perf_counter()
+            futs = []
+            for t_arr, r in reqs:
+                now = time.perf_counter() - t0
+                if t_arr > now:
+                    time.sleep(t_arr - now)
+                futs.append(srv.submit(**r))
+            for f in futs:
+                f.result()
+            wall = time.perf_counter() - t0
+            lat = srv.latencies()
+            srv.close()
+            row[name] = {"spectra_per_s": len(reqs) / wall,
+                         "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                         "p99_ms": float(np.percentile(lat, 99) * 1e3), "wall_s": wall}
+        results.append(row)
+    line = {"mode": "served", "metric": "spectra/s and latency under Poisson arrivals",
+            "slots": a.slots, "seconds_per_rate": a.seconds, "rates": results,
+            "config": {"dims": "{64,128,256,512} p=(.3,.3,.3,.1)", "particles_per_cell": "U{1..8}",
+                       "mas": "U{NGP,CIC,TSC,PCS}", "axis": "U{0,1,2}",
+                       "positions": "device-resident uniform pools", "hbm_budget_gb": 150}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.mode == "batched":
+        run_batched(a)
+    elif a.mode == "served":
+        run_served(a)
     else:
         run_ours(a)
 

@@ -14,8 +14,8 @@
  *   - Work is issued on the context's stream.  Calls with host outputs return
  *     after the results are on the host; calls with device outputs return
  *     once the work is enqueued (pyl_synchronize waits for it).
- *   - A context is used by one host thread at a time, except the serving
- *     calls (pyl_srv_*), which are thread safe.
+ *   - A context is used by one host thread at a time; concurrent requests
+ *     use one context each (pyl_pk_particles_enqueue / pyl_pk_collect).
  *
  * The reference interface each entry point replaces is cited beside it,
  * as path:line in the Pylians3 source tree.
@@ -165,6 +165,24 @@ int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n,
                      const float *W, int dims, float BoxSize, int mas_deposit,
                      int axis, int mas_window, int what, pyl_pk_out *out,
                      int flags);
+
+/* The same request split in two, for overlapping requests (one context per
+ * request in flight, each on its own stream):
+ *   enqueue -- issues all device work and the copy of the raw sums into
+ *              context-owned pinned memory, and returns at once (host
+ *              positions should then be pinned for the copy to be async);
+ *   query   -- 1 when the request has finished, 0 while in flight;
+ *   collect -- waits (timeout_ms >= 0 bounds the wait: PYL_ERR_TIMEOUT leaves
+ *              the request in flight; < 0 waits without bound) and writes the
+ *              finalised spectra into out.
+ * PYL_ERR_STATE: enqueue with a request already in flight, or query/collect
+ * without one.                                                             */
+int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n,
+                             const float *W, int dims, float BoxSize,
+                             int mas_deposit, int axis, int mas_window,
+                             int what, int flags);
+int pyl_pk_query(pyl_ctx *ctx);
+int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms);
 
 /* Power spectrum of a device grid without allocating device memory.
  * No counterpart in the reference: it exists for callers that cannot call

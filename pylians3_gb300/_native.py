@@ -41,6 +41,7 @@ EXPORTS = (
     "pyl_ctx_launch_count", "pyl_host_alloc", "pyl_host_free", "pyl_ma", "pyl_ma_f64",
     "pyl_fft_r2c", "pyl_fft_c2r", "pyl_pk_sizes", "pyl_pk", "pyl_pk_particles",
     "pyl_ctx_set_timing", "pyl_ctx_stage_times", "pyl_stage_name", "pyl_pk_noalloc",
+    "pyl_pk_particles_enqueue", "pyl_pk_query", "pyl_pk_collect",
 )
 
 
@@ -99,6 +100,9 @@ def load():
             "pyl_pk_noalloc": [vp, vp, i32, f64, i32, i32, i32, ctypes.POINTER(PkOut)],
             "pyl_pk_particles": [vp, vp, i64, vp, i32, f32, i32, i32, i32, i32,
                                  ctypes.POINTER(PkOut), i32],
+            "pyl_pk_particles_enqueue": [vp, vp, i64, vp, i32, f32, i32, i32, i32, i32, i32],
+            "pyl_pk_query": [vp],
+            "pyl_pk_collect": [vp, ctypes.POINTER(PkOut), i32],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)

@@ -40,6 +40,14 @@ struct ModeTables {
     long long total = 0;
 };
 
+// Device layout of the float64 sums of one Pk evaluation, followed by the raw
+// k = 0 mode (float2), the deposited mass (double) and the FFT shift (float).
+struct AccLayout {
+    size_t n3 = 0, n1 = 0, nph = 0, n2 = 0;
+    size_t sums() const { return sizeof(double) * (n3 + n1 + nph + n2); }
+    size_t bytes() const { return sums() + 64; }
+};
+
 // Accumulators of one Pk evaluation on the device (float64 sums).
 struct PkAcc {
     double *P3 = nullptr;     // (kmax+1)*3   sum of delta2 * L_ell(mu)
@@ -74,10 +82,22 @@ struct pyl_ctx {
     double stage_ms[ST_COUNT] = {};
     int64_t stage_n[ST_COUNT] = {};
 
+    // The request issued by pyl_pk_particles_enqueue and not yet collected:
+    // its raw sums are copied to `pinned` and `done` is recorded after them.
+    struct Request {
+        bool active = false;
+        int dims = 0, axis = 0, what = 0;
+        double BoxSize = 0.0;
+        const pyl::ModeTables *T = nullptr;
+        pyl::AccLayout L;
+    } req;
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+    cudaEvent_t done = nullptr;
+
     struct Buf { void *p = nullptr; size_t bytes = 0; };
     std::map<std::string, Buf> ws;                       // named workspaces
     std::map<int, pyl::FftPlan> fft;                     // per length
-    std::map<std::pair<int, int>, pyl::ModeTables> modes;  // per (dims, axis)
     std::map<std::pair<int, int>, float *> win;          // per (dims, mas)
 };
 
@@ -185,10 +205,6 @@ inline int isqrt_host(long long v) { return (int)__builtin_sqrt((double)v); }
 // ------------------------------------------------- spectrum bookkeeping (ctx.cu)
 // Device layout of the float64 sums of one Pk evaluation, followed by the raw
 // k = 0 mode (float2), the deposited mass (double) and the FFT shift (float).
-struct AccLayout {
-    size_t n3, n1, nph, n2;
-    size_t bytes() const { return sizeof(double) * (n3 + n1 + nph + n2) + 64; }
-};
 AccLayout acc_layout(const ModeTables &T);
 PkAcc acc_view(void *base, const AccLayout &L);
 // Finalisation of class Pk from the raw sums (host, float64).

@@ -6,6 +6,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <mutex>
+#include <thread>
 
 #include "common.cuh"
 
@@ -195,11 +198,20 @@ void mode_table_fill(ModeTables &T, const unsigned long long *h, size_t nn, size
     for (size_t i = 0; i < n2; ++i) T.N2D[i] = (double)h[nn + n1 + i];
 }
 
+// Mode tables are host data that depend only on (dims, axis): one cache for
+// the whole process, filled by whichever context needs a table first.  std::map
+// nodes are stable, so the returned pointers stay valid.
+static std::mutex g_modes_mu;
+static std::map<std::pair<int, int>, ModeTables> g_modes;
+
 const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status) {
     if (axis != 0 && axis != 1) axis = 2;
     auto key = std::make_pair(dims, axis);
-    auto it = ctx->modes.find(key);
-    if (it != ctx->modes.end()) return &it->second;
+    {
+        std::lock_guard<std::mutex> lock(g_modes_mu);
+        auto it = g_modes.find(key);
+        if (it != g_modes.end()) return &it->second;
+    }
     ModeTables T;
     size_t nn, n1, n2;
     mode_table_init(T, dims, axis, nn, n1, n2);
@@ -219,7 +231,9 @@ const ModeTables *mode_tables(pyl_ctx *ctx, int dims, int axis, int *status) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "mode count download"); return nullptr; }
     mode_table_fill(T, h.data(), nn, n1, n2);
-    return &(ctx->modes[key] = T);
+    std::lock_guard<std::mutex> lock(g_modes_mu);
+    auto ins = g_modes.emplace(key, std::move(T));   // a concurrent filler may have won
+    return &ins.first->second;
 }
 
 }  // namespace pyl
@@ -261,6 +275,13 @@ int pyl_ctx_destroy(pyl_ctx *ctx) {
     if (!ctx) return PYL_OK;
     cudaSetDevice(ctx->device);
     release_all(ctx);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->done) cudaEventDestroy(ctx->done);
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    for (auto &p : ctx->pending) {
+        cudaEventDestroy(p.a);
+        if (p.b) cudaEventDestroy(p.b);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PYL_OK;
@@ -679,9 +700,22 @@ int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n, const float *W, 
                      float BoxSize, int mas_deposit, int axis, int mas_window, int what,
                      pyl_pk_out *out, int flags) {
     if (!ctx) return PYL_ERR_ARG;
-    if (dims < 2 || !out || n <= 0 || !pos) return fail(ctx, PYL_ERR_ARG, "bad arguments");
+    if (!out) return fail(ctx, PYL_ERR_ARG, "null output");
+    const int st = pyl_pk_particles_enqueue(ctx, pos, n, W, dims, BoxSize, mas_deposit, axis,
+                                            mas_window, what, flags);
+    if (st) return st;
+    return pyl_pk_collect(ctx, out, -1);
+}
+
+int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const float *W,
+                             int dims, float BoxSize, int mas_deposit, int axis, int mas_window,
+                             int what, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (dims < 2 || n <= 0 || !pos) return fail(ctx, PYL_ERR_ARG, "bad arguments");
     if (mas_deposit < PYL_MAS_NGP || mas_deposit > PYL_MAS_PCS)
         return fail(ctx, PYL_ERR_ARG, "option not valid!!!");
+    if (ctx->req.active)
+        return fail(ctx, PYL_ERR_STATE, "a request is already in flight on this context");
     PYL_CUDA(ctx, cudaSetDevice(ctx->device));
     int st = PYL_OK;
     const ModeTables *T = mode_tables(ctx, dims, axis, &st);
@@ -718,19 +752,91 @@ int pyl_pk_particles(pyl_ctx *ctx, const float *pos, int64_t n, const float *W, 
     AccLayout L;
     const MassInfo mi{dW, n};
     if ((st = pk_device(ctx, grid, dims, axis, mas_window, what, *T, &acc, L, &mi))) return st;
-    std::vector<double> raw;
+    // raw sums, k = 0 mode and mass -> pinned host memory, then the event
+    const size_t nb = L.sums() + sizeof(float2) + sizeof(double);
+    if (ctx->pinned_bytes < nb) {
+        if (ctx->pinned) {
+            PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            cudaFreeHost(ctx->pinned);
+            ctx->pinned = nullptr;
+            ctx->pinned_bytes = 0;
+        }
+        PYL_CUDA(ctx, cudaHostAlloc(&ctx->pinned, nb, cudaHostAllocPortable));
+        ctx->pinned_bytes = nb;
+    }
+    if (!ctx->done) PYL_CUDA(ctx, cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming));
+    {
+        StageScope s(ctx, ST_D2H);
+        PYL_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, acc, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    PYL_CUDA(ctx, cudaEventRecord(ctx->done, ctx->stream));
+    ctx->req.active = true;
+    ctx->req.dims = dims;
+    ctx->req.axis = axis;
+    ctx->req.what = what;
+    ctx->req.BoxSize = BoxSize;
+    ctx->req.T = T;
+    ctx->req.L = L;
+    return PYL_OK;
+}
+
+int pyl_pk_query(pyl_ctx *ctx) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (!ctx->req.active) return fail(ctx, PYL_ERR_STATE, "no request in flight");
+    const cudaError_t e = cudaEventQuery(ctx->done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return cuda_fail(ctx, e, "cudaEventQuery");
+}
+
+}  // extern "C"
+
+namespace {
+// Wait for the event with a bound; timeout_ms < 0 waits without one.
+int wait_done(pyl_ctx *ctx, int timeout_ms) {
+    if (timeout_ms < 0) {
+        PYL_CUDA(ctx, cudaEventSynchronize(ctx->done));
+        return PYL_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t e = cudaEventQuery(ctx->done);
+        if (e == cudaSuccess) return PYL_OK;
+        if (e != cudaErrorNotReady) return cuda_fail(ctx, e, "cudaEventQuery");
+        const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+                            std::chrono::steady_clock::now() - t0).count();
+        if (ms >= timeout_ms) return fail(ctx, PYL_ERR_TIMEOUT, "request not finished in time");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (!out) return fail(ctx, PYL_ERR_ARG, "null output");
+    if (!ctx->req.active) return fail(ctx, PYL_ERR_STATE, "no request in flight");
+    int st = wait_done(ctx, timeout_ms);
+    if (st) return st;   // a timeout leaves the request in flight
+    ctx->req.active = false;
+    const pyl_ctx::Request &R = ctx->req;
+    const AccLayout &L = R.L;
+    std::vector<double> raw(L.n3 + L.n1 + L.nph + L.n2 + 8);
+    memcpy(raw.data(), ctx->pinned, L.sums());
     float2 dc;
     double mass;
-    if ((st = download_raw(ctx, acc, L, raw, &dc, &mass))) return st;
+    memcpy(&dc, (const char *)ctx->pinned + L.sums(), sizeof(float2));
+    memcpy(&mass, (const char *)ctx->pinned + L.sums() + sizeof(float2), sizeof(double));
     // The FFT saw rho - shift (shift = mass per cell rounded to float, as on
     // the device); the grid mean is shift + DC / dims^3, and
     // P(delta = rho/mean - 1) = P(rho) / mean^2 for every k != 0.
-    const double cells = (double)dims * dims * dims;
+    const double cells = (double)R.dims * R.dims * R.dims;
     const double shift = (double)(float)(mass * (1.0 / cells));
     const double mean = shift + (double)dc.x / cells;
     if (!(mean > 0.0) && !(mean < 0.0))
         return fail(ctx, PYL_ERR_ARG, "grid mean is zero: cannot form the overdensity");
-    return finalize(ctx, *T, raw, L, BoxSize, what, 1.0 / (mean * mean), true, out);
+    return finalize(ctx, *R.T, raw, L, R.BoxSize, R.what, 1.0 / (mean * mean), true, out);
 }
 
 }  // extern "C"

@@ -1,0 +1,101 @@
+"""Split request API (enqueue / query / collect) and the continuous-batching
+server: every request's spectrum is the same alone and in a mix of
+concurrent requests (|dP_ell| / |P0| <= 1e-5 per bin: only the order of
+floating-point atomic additions differs), admission by HBM budget, bounded
+waits."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BOX = 1000.0
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    assert torch.cuda.is_available()
+    from pylians3_gb300 import build_native, _native
+    build_native.build()
+    import pylians3_gb300 as P
+    return torch, _native, P
+
+
+def pk_err(a, b):
+    return float((np.abs(a - b).max(axis=1) / np.abs(b[:, 0])).max())
+
+
+def make_pos(torch, n, seed):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    return torch.rand((n, 3), generator=g, device="cuda") * BOX
+
+
+def test_enqueue_collect_equals_blocking_call(env):
+    torch, native, P = env
+    from pylians3_gb300.Pk_library import _Outputs
+    ctx = native.Context(0)
+    pos = make_pos(torch, 1 << 20, 1)
+    torch.cuda.synchronize()
+    ref = P.power_spectrum(pos, 64, BOX, "CIC", axis=1, ctx=ctx)
+    out = _Outputs(64, 0)
+    p = ctypes.c_void_p(pos.data_ptr())
+    assert ctx.lib.pyl_pk_query(ctx.ptr) == native.PYL_ERR_STATE
+    ctx.check(ctx.lib.pyl_pk_particles_enqueue(ctx.ptr, p, pos.shape[0], None, 64,
+                                                ctypes.c_float(BOX), 2, 1, 2, 0,
+                                                native.PYL_DEVICE_PTRS))
+    # a second request on the same context is refused while one is in flight
+    assert ctx.lib.pyl_pk_particles_enqueue(ctx.ptr, p, pos.shape[0], None, 64,
+                                             ctypes.c_float(BOX), 2, 1, 2, 0,
+                                             native.PYL_DEVICE_PTRS) == native.PYL_ERR_STATE
+    rc = ctx.lib.pyl_pk_collect(ctx.ptr, ctypes.byref(out.struct), 0)   # bounded: may time out
+    assert rc in (native.PYL_OK, native.PYL_ERR_TIMEOUT)
+    if rc == native.PYL_ERR_TIMEOUT:
+        ctx.check(ctx.lib.pyl_pk_collect(ctx.ptr, ctypes.byref(out.struct), -1))
+    assert pk_err(out.Pk, ref.Pk) <= 1e-5
+    assert np.array_equal(out.Nmodes3D, ref.Nmodes3D)
+    assert ctx.lib.pyl_pk_collect(ctx.ptr, ctypes.byref(out.struct), -1) == native.PYL_ERR_STATE
+    ctx.close()
+
+
+def test_server_mix_equals_alone(env):
+    torch, native, P = env
+    from pylians3_gb300.serving import Server
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(14):
+        dims = int(rng.choice([32, 48, 64, 128]))
+        n = int(dims ** 3 * rng.integers(1, 4))
+        reqs.append(dict(pos=make_pos(torch, n, 100 + i), dims=dims, BoxSize=BOX,
+                         MAS=str(rng.choice(["NGP", "CIC", "TSC", "PCS"])),
+                         axis=int(rng.integers(0, 3))))
+    torch.cuda.synchronize()
+    alone = [P.power_spectrum(**r) for r in reqs]
+    srv = Server(slots=6, hbm_budget=40e9)
+    futs = [srv.submit(**r) for r in reqs]
+    mixed = [f.result(timeout=300) for f in futs]
+    srv.close()
+    for a, m in zip(alone, mixed):
+        assert np.array_equal(a.Nmodes3D, m.Nmodes3D)
+        np.testing.assert_allclose(a.k3D, m.k3D, rtol=1e-12)
+        assert pk_err(m.Pk, a.Pk) <= 1e-5
+    assert len(srv.latencies()) == len(reqs)
+
+
+def test_server_budget(env):
+    torch, native, P = env
+    from pylians3_gb300.serving import Server, request_bytes
+    pos = make_pos(torch, 1 << 20, 7)
+    torch.cuda.synchronize()
+    need = request_bytes(1 << 20, 64, False, False)
+    # room for one request at a time: all complete, one after another
+    srv = Server(slots=4, hbm_budget=int(need * 1.5))
+    futs = [srv.submit(pos, 64, BOX, "CIC", axis=2) for _ in range(5)]
+    res = [f.result(timeout=300) for f in futs]
+    ref = P.power_spectrum(pos, 64, BOX, "CIC", axis=2)
+    for r in res:
+        assert pk_err(r.Pk, ref.Pk) <= 1e-5
+    with pytest.raises(native.PylError):
+        srv.submit(make_pos(torch, 1 << 22, 8), 128, BOX, "CIC")
+    srv.close()
