@@ -97,8 +97,6 @@ struct pyl_ctx {
 
     struct Buf { void *p = nullptr; size_t bytes = 0; };
     std::map<std::string, Buf> ws;                       // named workspaces
-    std::map<int, pyl::FftPlan> fft;                     // per length
-    std::map<std::pair<int, int>, float *> win;          // per (dims, mas)
 };
 
 namespace pyl {
@@ -156,10 +154,9 @@ inline int scale_any(pyl_ctx *ctx, double *g, int64_t c, double s) {
     return scale_grid_f64(ctx, g, c, s);
 }
 
-// fft.cu (power-of-two lengths go to fft_pow2.cu)
+// fft.cu (lengths 2^k and 3*2^k go to fft_reg.cu)
 // r2c along the last axis of rows (rows x n real -> rows x (n/2+1) complex,
-// output row stride ostride >= n/2+1; padding needs a power-of-two n)
-// output row stride ostride >= n/2+1; padding needs a power-of-two n).  When
+// output row stride ostride >= n/2+1; padding needs n = 2^k or 3*2^k).  When
 // shift is not null, *shift (device) is subtracted from every input value
 // (changes only the k = 0 mode, and keeps its round-off out of the others).
 int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
@@ -171,8 +168,8 @@ int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n
 // rows have stride rs >= h
 int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int dir);
 
-// fft_pow2.cu
-bool pow2_supported(int n);
+// fft_reg.cu: lengths 2^k (16..4096) and 3*2^k (48..3072)
+bool reg_supported(int n);
 int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
                   const float2 *tw, const float *shift);
 // total mass (sum of W, or n) into *mass, then *shift = mass / cells
@@ -194,7 +191,7 @@ int pk_bin_x(pyl_ctx *ctx, const float2 *data, int n, int rs, int axis, int mas,
 // on the power-of-two path)
 inline int half_stride(int n) {
     const int h = n / 2 + 1;
-    return (n >= 16 && (n & (n - 1)) == 0) ? (h + 7) / 8 * 8 : h;
+    return reg_supported(n) ? (h + 7) / 8 * 8 : h;
 }
 // integer mode counts of (dims, axis) into device histograms
 int mode_counts(pyl_ctx *ctx, int dims, int axis, unsigned long long *cnt_n,

@@ -32,6 +32,7 @@ int cuda_fail(pyl_ctx *ctx, cudaError_t e, const char *what) {
 void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status) {
     pyl_ctx::Buf &b = ctx->ws[name];
     if (b.bytes >= bytes && b.p) return b.p;
+    const size_t old = b.p ? b.bytes : 0;
     if (b.p) {
         // the stream may still use the old buffer
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -41,6 +42,9 @@ void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status) {
         b.bytes = 0;
     }
     size_t want = bytes < 256 ? 256 : bytes;
+    // growing workspaces grow by at least 25 %, so that requests of slowly
+    // increasing size do not reallocate (and synchronise) every time
+    if (old && want < old + old / 4) want = old + old / 4;
     cudaError_t e = cudaMalloc(&b.p, want);
     if (e != cudaSuccess) {
         b.p = nullptr;
@@ -125,9 +129,19 @@ static void factorize(int n, FftDesc &D) {
     if (m > 1) D.radix[D.nst++] = m;
 }
 
+// FFT plans and window tables are small read-only device tables that depend
+// only on (device, size[, scheme]): one cache for the whole process, so that
+// contexts serving requests side by side do not create (and synchronise on)
+// their own copies.  They live until the process exits.
+static std::mutex g_tables_mu;
+static std::map<std::pair<int, int>, FftPlan> g_fft;                 // (device, n)
+static std::map<std::tuple<int, int, int>, float *> g_win;           // (device, dims, mas)
+
 const FftPlan *fft_plan(pyl_ctx *ctx, int n, int *status) {
-    auto it = ctx->fft.find(n);
-    if (it != ctx->fft.end()) return &it->second;
+    const auto key = std::make_pair(ctx->device, n);
+    std::lock_guard<std::mutex> lock(g_tables_mu);
+    auto it = g_fft.find(key);
+    if (it != g_fft.end()) return &it->second;
     FftPlan P;
     factorize(n, P.desc);
     std::vector<float2> tw;
@@ -136,16 +150,17 @@ const FftPlan *fft_plan(pyl_ctx *ctx, int n, int *status) {
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle table"); return nullptr; }
     e = cudaMemcpy(P.d_tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle upload"); return nullptr; }
-    return &(ctx->fft[n] = P);
+    return &(g_fft[key] = P);
 }
 
 // MAS_correction (Pk_library.pyx:83-84): 1 if x == 0 else (x / sin x)^p,
 // x = pi * k / dims with k the signed frequency of index i.
 const float *window_table(pyl_ctx *ctx, int dims, int mas, int *status) {
     if (mas < 1 || mas > 4) mas = 0;
-    auto key = std::make_pair(dims, mas);
-    auto it = ctx->win.find(key);
-    if (it != ctx->win.end()) return it->second;
+    const auto key = std::make_tuple(ctx->device, dims, mas);
+    std::lock_guard<std::mutex> lock(g_tables_mu);
+    auto it = g_win.find(key);
+    if (it != g_win.end()) return it->second;
     std::vector<float> w;
     window_host(dims, mas, w);
     float *d = nullptr;
@@ -153,7 +168,7 @@ const float *window_table(pyl_ctx *ctx, int dims, int mas, int *status) {
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "window table"); return nullptr; }
     e = cudaMemcpy(d, w.data(), sizeof(float) * dims, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "window upload"); return nullptr; }
-    ctx->win[key] = d;
+    g_win[key] = d;
     return d;
 }
 
@@ -265,10 +280,6 @@ static void release_all(pyl_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto &kv : ctx->ws) if (kv.second.p) cudaFree(kv.second.p);
     ctx->ws.clear();
-    for (auto &kv : ctx->fft) cudaFree(kv.second.d_tw);
-    ctx->fft.clear();
-    for (auto &kv : ctx->win) cudaFree(kv.second);
-    ctx->win.clear();
 }
 
 int pyl_ctx_destroy(pyl_ctx *ctx) {
@@ -321,7 +332,6 @@ int pyl_ctx_workspace_bytes(const pyl_ctx *ctx, size_t *bytes) {
     if (!ctx || !bytes) return PYL_ERR_ARG;
     size_t s = 0;
     for (auto &kv : ctx->ws) s += kv.second.bytes;
-    for (auto &kv : ctx->fft) s += sizeof(float2) * kv.second.desc.n;
     *bytes = s;
     return PYL_OK;
 }

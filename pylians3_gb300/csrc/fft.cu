@@ -132,7 +132,7 @@ int fft_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
-    if (pow2_supported(n)) return pow2_rows_r2c(ctx, in, out, rows, n, ostride, P->d_tw, shift);
+    if (reg_supported(n)) return pow2_rows_r2c(ctx, in, out, rows, n, ostride, P->d_tw, shift);
     if (ostride != n / 2 + 1) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     int pairs = (int)(kLineBudget / (sizeof(float2) * (size_t)n));
     if (pairs < 1) pairs = 1;
@@ -154,7 +154,7 @@ int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
-    if (pow2_supported(n)) return pow2_rows_c2r(ctx, in, out, rows, n, istride, P->d_tw, scale);
+    if (reg_supported(n)) return pow2_rows_c2r(ctx, in, out, rows, n, istride, P->d_tw, scale);
     if (istride != n / 2 + 1) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     int pairs = (int)(kLineBudget / (sizeof(float2) * (size_t)n));
     if (pairs < 1) pairs = 1;
@@ -175,7 +175,7 @@ int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);
     if (!P) return st;
-    if (pow2_supported(n)) {
+    if (reg_supported(n)) {
         const int64_t plane = (int64_t)n * rs;
         return axis == 1 ? pow2_cols(ctx, data, n, h, rs, plane, n, dir, P->d_tw)
                          : pow2_cols(ctx, data, n, h, plane, rs, n, dir, P->d_tw);

@@ -1,6 +1,6 @@
-// Power-of-two fast path of the 3D FFT passes and of the fused power-spectrum
-// pass (the generic mixed-radix kernels in fft.cu / pk.cu handle every other
-// length).  See fft_pow2.cuh for the register-resident FFT.
+// Fast path (lengths 2^k and 3*2^k) of the 3D FFT passes and of the fused
+// power-spectrum pass (the generic mixed-radix kernels in fft.cu / pk.cu
+// handle every other length).  See fft_reg.cuh for the register-resident FFT.
 //
 //   rows r2c / c2r : a CTA transforms L row pairs (a + i b) of length N;
 //                    loads and stores are contiguous runs along z.
@@ -11,10 +11,10 @@
 //                    natural-order result the same way.
 //   pk_x           : the x-column transform fused with the window, |delta|^2,
 //                    Legendre weights and the integer-|k| binning, straight
-//                    from registers; persistent CTAs, float32 shared
-//                    histograms folded into float64 shared sums every few
-//                    items, one float64 atomic per bin and CTA at the end.
-#include "fft_pow2.cuh"
+//                    via a padded shared line; a CTA bins a few items into
+//                    float32 shared histograms and adds them to the float64
+//                    sums when it ends.
+#include "fft_reg.cuh"
 #include "pk_common.cuh"
 
 namespace pyl {
@@ -23,16 +23,20 @@ namespace {
 
 template <int N>
 struct RowsCfg {
-    static constexpr int P = N / 8;
+    static constexpr int P = RegPlan<N>::P;
     static constexpr int L = P >= 256 ? 1 : 256 / P;   // row pairs per CTA
     static constexpr int THREADS = L * P;
 };
 
 template <int N>
 struct ColsCfg {
-    static constexpr int P = N / 8;
+    static constexpr int P = RegPlan<N>::P;
     static constexpr int C = P >= 512 ? 1 : (512 / P > 8 ? 8 : 512 / P);
     static constexpr int THREADS = C * P;
+    // resident CTAs the fused Pk kernel is compiled for: E = 12 keeps two
+    // register lines (the current item and the prefetched one) per thread
+    static constexpr int PK_MINB =
+        RegPlan<N>::E == 8 ? (THREADS >= 512 ? 2 : 4) : (THREADS >= 512 ? 1 : 2);
 };
 
 template <int N>
@@ -40,7 +44,7 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
 k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t rows, int ostride,
               const float2 *__restrict__ g_tw, const float *__restrict__ shift) {
     using CF = RowsCfg<N>;
-    constexpr int P = CF::P, LINE = Pow2<N>::LINE, H = N / 2 + 1;
+    constexpr int P = CF::P, LINE = RegPlan<N>::LINE, H = N / 2 + 1;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     const int l = threadIdx.x / P, t = threadIdx.x % P;
@@ -48,9 +52,9 @@ k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t ro
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
     const float sh = shift ? *shift : 0.f;
     const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
-    float2 v[8];
+    float2 v[RegPlan<N>::E];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
+    for (int s = 0; s < RegPlan<N>::E; ++s) {
         const float a = ra < rows ? __ldcs(in + ra * N + t + s * P) - sh : 0.f;
         const float b = rb < rows ? __ldcs(in + rb * N + t + s * P) - sh : 0.f;
         v[s] = make_float2(a, b);
@@ -58,11 +62,11 @@ k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t ro
     __syncthreads();
     fft_line<N, -1>(v, t, line, tw);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) line[pad8(t + u * P)] = v[u];
+    for (int u = 0; u < RegPlan<N>::E; ++u) line[pad8(t + u * P)] = v[u];
     __syncthreads();
     for (int k = t; k < H; k += P) {
         const float2 Z = line[pad8(k)];
-        const float2 Zm = line[pad8((N - k) & (N - 1))];
+        const float2 Zm = line[pad8(k == 0 ? 0 : N - k)];
         if (ra < rows)
             out[ra * ostride + k] = make_float2(0.5f * (Z.x + Zm.x), 0.5f * (Z.y - Zm.y));
         if (rb < rows)
@@ -75,16 +79,16 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
 k_rows_c2r_p2(const float2 *__restrict__ in, float *__restrict__ out, int64_t rows, int istride,
               const float2 *__restrict__ g_tw, float scale) {
     using CF = RowsCfg<N>;
-    constexpr int P = CF::P, LINE = Pow2<N>::LINE, H = N / 2 + 1;
+    constexpr int P = CF::P, LINE = RegPlan<N>::LINE, H = N / 2 + 1;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     const int l = threadIdx.x / P, t = threadIdx.x % P;
     float2 *line = sm + N + l * LINE;
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
     const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
-    float2 v[8];
+    float2 v[RegPlan<N>::E];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
+    for (int s = 0; s < RegPlan<N>::E; ++s) {
         const int k = t + s * P;
         const bool lower = k < H;
         const int kk = lower ? k : N - k;
@@ -97,7 +101,7 @@ k_rows_c2r_p2(const float2 *__restrict__ in, float *__restrict__ out, int64_t ro
     __syncthreads();
     fft_line<N, +1>(v, t, line, tw);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < RegPlan<N>::E; ++u) {
         if (ra < rows) out[ra * N + t + u * P] = v[u].x * scale;
         if (rb < rows) out[rb * N + t + u * P] = v[u].y * scale;
     }
@@ -110,7 +114,7 @@ __global__ void __launch_bounds__(ColsCfg<N>::THREADS, 1)
 k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
           const float2 *__restrict__ g_tw) {
     using CF = ColsCfg<N>;
-    constexpr int P = CF::P, C = CF::C, LINE = Pow2<N>::LINE;
+    constexpr int P = CF::P, C = CF::C, LINE = RegPlan<N>::LINE;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
@@ -119,15 +123,15 @@ k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
     const int col = blockIdx.x * C + c;
     const bool valid = col < ncol;
     float2 *base = data + (int64_t)blockIdx.y * ostride + col;
-    float2 v[8];
+    float2 v[RegPlan<N>::E];
 #pragma unroll
-    for (int s = 0; s < 8; ++s)
+    for (int s = 0; s < RegPlan<N>::E; ++s)
         v[s] = valid ? base[(int64_t)(t + s * P) * estride] : make_float2(0.f, 0.f);
     __syncthreads();
     fft_line<N, DIR>(v, t, line, tw);
     if (valid) {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) base[(int64_t)(t + u * P) * estride] = v[u];
+        for (int u = 0; u < RegPlan<N>::E; ++u) base[(int64_t)(t + u * P) * estride] = v[u];
     }
 }
 
@@ -135,11 +139,11 @@ k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
 // (kyy, kz block) into float32 shared histograms (a few hundred terms per bin
 // at most) and adds them to the float64 sums when it ends.
 template <int N, int WHAT>
-__global__ void __launch_bounds__(ColsCfg<N>::THREADS, (ColsCfg<N>::THREADS >= 512 ? 2 : 4))
+__global__ void __launch_bounds__(ColsCfg<N>::THREADS, ColsCfg<N>::PK_MINB)
 k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restrict__ g_tw,
           const float *__restrict__ g_win, int axis, int kmax, PkAcc acc, int nitems, int ipb) {
     using CF = ColsCfg<N>;
-    constexpr int P = CF::P, C = CF::C, LINE = Pow2<N>::LINE;
+    constexpr int P = CF::P, C = CF::C, LINE = RegPlan<N>::LINE;
     constexpr int MID = N / 2;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
@@ -155,24 +159,24 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
     const int it0 = blockIdx.x * ipb;
     const int it1 = min(nitems, it0 + ipb);
     // column c of item `item`, element s of thread t -> registers
-    auto load = [&](int item, float2 (&v)[8]) {
+    auto load = [&](int item, float2 (&v)[RegPlan<N>::E]) {
         const int kz = (item % nzb) * C + c;
         const bool valid = kz < h;
         const float2 *base = data + (int64_t)(item / nzb) * rs + kz;
         const int64_t es = (int64_t)N * rs;
 #pragma unroll
-        for (int s = 0; s < 8; ++s)
+        for (int s = 0; s < RegPlan<N>::E; ++s)
             v[s] = valid ? __ldcs(base + (int64_t)(t + s * P) * es) : make_float2(0.f, 0.f);
     };
-    float2 v[8];
+    float2 v[RegPlan<N>::E];
     if (it0 < it1) load(it0, v);
     for (int it = it0; it < it1; ++it) {
         const int kyy = it / nzb;
         fft_line<N, -1>(v, t, line, tw);
-        // natural order into the line, then each thread bins a run of 8
+        // natural order into the line, then each thread bins a run of E
         // consecutive kx of one column (neighbouring lanes -> different bins)
 #pragma unroll
-        for (int u = 0; u < 8; ++u) line[pad8(t + u * P)] = v[u];
+        for (int u = 0; u < RegPlan<N>::E; ++u) line[pad8(t + u * P)] = v[u];
         __syncthreads();
         // the next item's loads are in flight while this one is binned
         if (it + 1 < it1) load(it + 1, v);
@@ -183,8 +187,9 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
                 const float2 *ln = sm + N + cc * LINE;
                 const int ky = kyy > MID ? kyy - N : kyy;
                 const float wyz = win[kyy] * win[kzc];
-                bin_run8<WHAT>(H, acc, ln, [](int i) { return pad8(i); }, 8 * rr, ky, kzc, N,
-                               axis, win, wyz, MID);
+                constexpr int E = RegPlan<N>::E;
+                bin_run<WHAT, E>(H, acc, ln, [](int i) { return pad8(i); }, E * rr, ky, kzc, N,
+                                 axis, win, wyz, MID);
             }
         }
         __syncthreads();   // the shared lines are reused by the next item
@@ -204,7 +209,7 @@ template <int N>
 int rows_r2c_n(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int ostride,
                const float2 *tw, const float *shift) {
     using CF = RowsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * Pow2<N>::LINE);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * RegPlan<N>::LINE);
     int st;
     if ((st = set_smem(ctx, k_rows_r2c_p2<N>, smem))) return st;
     const int64_t pairs = (rows + 1) / 2;
@@ -220,7 +225,7 @@ template <int N>
 int rows_c2r_n(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int istride,
                const float2 *tw, float scale) {
     using CF = RowsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * Pow2<N>::LINE);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * RegPlan<N>::LINE);
     int st;
     if ((st = set_smem(ctx, k_rows_c2r_p2<N>, smem))) return st;
     const int64_t pairs = (rows + 1) / 2;
@@ -236,7 +241,7 @@ template <int N>
 int cols_n(pyl_ctx *ctx, float2 *data, int ncol, int64_t estride, int64_t ostride, int nouter,
            int dir, const float2 *tw) {
     using CF = ColsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * Pow2<N>::LINE);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE);
     int st;
     dim3 grid((ncol + CF::C - 1) / CF::C, nouter);
     if (dir < 0) {
@@ -255,7 +260,7 @@ template <int N, int WHAT>
 int pk_n(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const float2 *tw,
          const float *win, int kmax, const PkAcc &acc) {
     using CF = ColsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * Pow2<N>::LINE) +
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE) +
                         sizeof(float) * N + FltHist::bytes(kmax, N / 2, WHAT);
     if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "Pk histogram too large");
     int st;
@@ -291,7 +296,15 @@ int pk_what(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const flo
 
 }  // namespace
 
-bool pow2_supported(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
+bool reg_supported(int n) {
+    switch (n) {
+        case 16: case 32: case 64: case 128: case 256: case 512: case 1024: case 2048:
+        case 4096: case 48: case 96: case 192: case 384: case 768: case 1536: case 3072:
+            return true;
+        default:
+            return false;
+    }
+}
 
 #define PYL_POW2_DISPATCH(n, CALL)                 \
     switch (n) {                                   \
@@ -304,6 +317,13 @@ bool pow2_supported(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; 
         case 1024: return CALL(1024);              \
         case 2048: return CALL(2048);              \
         case 4096: return CALL(4096);              \
+        case 48: return CALL(48);                  \
+        case 96: return CALL(96);                  \
+        case 192: return CALL(192);                \
+        case 384: return CALL(384);                \
+        case 768: return CALL(768);                \
+        case 1536: return CALL(1536);              \
+        case 3072: return CALL(3072);              \
         default: return PYL_ERR_UNSUPPORTED;       \
     }
 

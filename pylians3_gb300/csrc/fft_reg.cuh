@@ -1,0 +1,170 @@
+// Register-resident Stockham FFT for lengths N = 2^k (N >= 16) and
+// N = 3 * 2^k (N >= 48).
+//
+// A line of N complex values is held by P = N/E threads, thread t owning
+// x[t + s*P], s = 0..E-1 ("strided" layout); E = 8 for powers of two and
+// E = 12 for 3 * 2^k.  A stage of radix R (R divides E) with Ns = product of
+// the earlier radices performs, for every butterfly j in [0, N/R),
+//     k = j mod Ns,  x_q = in[j + q*N/R] * W^(k*q),  W = exp(dir*2*pi*i/(Ns*R))
+//     out[(j - k)*R + k + u*Ns] = sum_q x_q exp(dir*2*pi*i*u*q/R)
+// Thread t runs butterflies j = t + b*P (b < E/R), whose inputs are exactly
+// its registers v[b + q*(E/R)]; outputs go through shared memory to the next
+// stage.  In the last stage Ns = N/R, so its outputs land in the strided
+// layout again in natural order: thread t ends with X[t + u*P] and no final
+// exchange is needed.  Stage radices:
+//   2^k    : one 2 or 4 first when k is not a multiple of 3, then 8s;
+//   3*2^k  : a 3 first, then 4s, then a 2 when k is odd.
+// Shared-memory indices are padded by one element every 8 (pad8) so that
+// the strided stores of the first stage do not conflict on banks.
+#pragma once
+
+#include "fft_core.cuh"
+
+namespace pyl {
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+template <int N>
+struct RegPlan {
+    static constexpr bool POW2 = (N & (N - 1)) == 0;
+    static constexpr int E = POW2 ? 8 : 12;
+    static constexpr int P = N / E;
+    static constexpr int LINE = N + N / 8 + 1;   // padded line stride in shared memory
+    static constexpr int K = POW2 ? ilog2c(N) : ilog2c(N / 3);   // power of two part
+    static constexpr int NST = POW2 ? (K % 3 == 0 ? K / 3 : K / 3 + 1)
+                                    : 1 + K / 2 + (K % 2);
+    static constexpr int radix(int s) {
+        if (POW2) return (s == 0 && K % 3 != 0) ? (K % 3 == 1 ? 2 : 4) : 8;
+        if (s == 0) return 3;
+        return (s == NST - 1 && (K % 2)) ? 2 : 4;
+    }
+    static constexpr int ns(int s) { return s == 0 ? 1 : ns(s - 1) * radix(s - 1); }
+};
+
+template <int N>
+constexpr bool reg_fft_length() {
+    return (N >= 16 && (N & (N - 1)) == 0) ||
+           (N >= 48 && N % 3 == 0 && ((N / 3) & (N / 3 - 1)) == 0);
+}
+
+__device__ __forceinline__ int pad8(int i) { return i + (i >> 3); }
+
+template <int DIR>
+__device__ __forceinline__ float2 twl(const float2 *tw, int m) {
+    float2 w = tw[m];
+    if (DIR > 0) w.y = -w.y;
+    return w;
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft3(float2 &a0, float2 &a1, float2 &a2) {
+    const float h3 = 0.86602540378443864676f;   // sqrt(3)/2
+    const float2 t1 = cadd(a1, a2), t2 = csub(a1, a2);
+    const float2 m = make_float2(a0.x - 0.5f * t1.x, a0.y - 0.5f * t1.y);
+    const float2 r = mul_i<DIR>(make_float2(h3 * t2.x, h3 * t2.y));
+    a0 = cadd(a0, t1);
+    a1 = cadd(m, r);
+    a2 = csub(m, r);
+}
+
+// One stage in registers.
+template <int N, int R, int NS, int DIR>
+__device__ __forceinline__ void stage_compute(float2 (&v)[RegPlan<N>::E], int t, const float2 *tw) {
+    constexpr int E = RegPlan<N>::E;
+    constexpr int P = RegPlan<N>::P;
+    constexpr int NB = E / R;
+    constexpr int ST = N / (NS * R);   // table stride of W
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = t + b * P;
+        const int k = j % NS;
+        float2 x[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) x[q] = v[b + q * NB];
+        if constexpr (NS > 1) {
+            if constexpr (R == 2) {
+                x[1] = cmul(x[1], twl<DIR>(tw, k * ST));
+            } else if constexpr (R == 3) {
+                x[1] = cmul(x[1], twl<DIR>(tw, k * ST));
+                x[2] = cmul(x[2], twl<DIR>(tw, 2 * k * ST));
+            } else if constexpr (R == 4) {
+                const float2 w1 = twl<DIR>(tw, k * ST), w2 = twl<DIR>(tw, 2 * k * ST);
+                x[1] = cmul(x[1], w1);
+                x[2] = cmul(x[2], w2);
+                x[3] = cmul(x[3], cmul(w1, w2));
+            } else {
+                const float2 w1 = twl<DIR>(tw, k * ST), w2 = twl<DIR>(tw, 2 * k * ST);
+                const float2 w4 = twl<DIR>(tw, 4 * k * ST);
+                const float2 w3 = cmul(w1, w2);
+                x[1] = cmul(x[1], w1);
+                x[2] = cmul(x[2], w2);
+                x[3] = cmul(x[3], w3);
+                x[4] = cmul(x[4], w4);
+                x[5] = cmul(x[5], cmul(w1, w4));
+                x[6] = cmul(x[6], cmul(w2, w4));
+                x[7] = cmul(x[7], cmul(w3, w4));
+            }
+        }
+        if constexpr (R == 2) dft2<DIR>(x[0], x[1]);
+        else if constexpr (R == 3) dft3<DIR>(x[0], x[1], x[2]);
+        else if constexpr (R == 4) dft4<DIR>(x[0], x[1], x[2], x[3]);
+        else dft8<DIR>(x);
+#pragma unroll
+        for (int u = 0; u < R; ++u) v[b + u * NB] = x[u];
+    }
+}
+
+// Scatter the stage outputs to their Stockham positions in the shared line.
+template <int N, int R, int NS>
+__device__ __forceinline__ void stage_store(const float2 (&v)[RegPlan<N>::E], int t, float2 *line) {
+    constexpr int E = RegPlan<N>::E;
+    constexpr int P = RegPlan<N>::P;
+    constexpr int NB = E / R;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = t + b * P;
+        const int k = j % NS;
+        const int ob = (j - k) * R + k;
+#pragma unroll
+        for (int u = 0; u < R; ++u) line[pad8(ob + u * NS)] = v[b + u * NB];
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void strided_load(float2 (&v)[RegPlan<N>::E], int t, const float2 *line) {
+    constexpr int E = RegPlan<N>::E;
+    constexpr int P = RegPlan<N>::P;
+#pragma unroll
+    for (int s = 0; s < E; ++s) v[s] = line[pad8(t + s * P)];
+}
+
+// Stage S of the plan (compile-time recursion).  Each exchange between
+// stages is bracketed by __syncthreads(), so every thread of the CTA must
+// call this the same number of times.
+template <int N, int DIR, int S>
+__device__ __forceinline__ void run_stages(float2 (&v)[RegPlan<N>::E], int t, float2 *line,
+                                           const float2 *tw) {
+    using PL = RegPlan<N>;
+    constexpr int R = PL::radix(S);
+    constexpr int NS = PL::ns(S);
+    stage_compute<N, R, NS, DIR>(v, t, tw);
+    if constexpr (S + 1 < PL::NST) {
+        stage_store<N, R, NS>(v, t, line);
+        __syncthreads();
+        strided_load<N>(v, t, line);
+        __syncthreads();
+        run_stages<N, DIR, S + 1>(v, t, line, tw);
+    }
+}
+
+// Full FFT of the thread's line: input and output in the strided layout.
+template <int N, int DIR>
+__device__ __forceinline__ void fft_line(float2 (&v)[RegPlan<N>::E], int t, float2 *line,
+                                         const float2 *tw) {
+    static_assert(reg_fft_length<N>(), "register FFT length must be 2^k or 3*2^k");
+    static_assert(RegPlan<N>::ns(RegPlan<N>::NST - 1) * RegPlan<N>::radix(RegPlan<N>::NST - 1) == N,
+                  "stage radices must multiply to N");
+    run_stages<N, DIR, 0>(v, t, line, tw);
+}
+
+}  // namespace pyl

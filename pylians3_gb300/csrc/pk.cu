@@ -5,7 +5,7 @@
 // bin_mode() in pk_common.cuh.
 //
 // Input: the (n, n, h) half-complex grid already transformed along z and y.
-// Power-of-two n takes the register-resident kernel of fft_pow2.cu; this file
+// Lengths 2^k and 3*2^k take the register-resident kernel of fft_reg.cu; this file
 // holds the generic (any n) kernel: a CTA owns one ky row and a block of B
 // consecutive kz columns, loads the B pencils along x (runs of B*8
 // contiguous bytes), transforms them in shared memory and bins every mode.
@@ -129,7 +129,7 @@ int pk_bin_x(pyl_ctx *ctx, const float2 *data, int n, int rs, int axis, int mas,
     if (!P) return st;
     const float *win = window_table(ctx, n, mas, &st);
     if (!win) return st;
-    if (pow2_supported(n)) return pow2_pk_x(ctx, data, n, rs, axis, P->d_tw, win, kmax, acc, what);
+    if (reg_supported(n)) return pow2_pk_x(ctx, data, n, rs, axis, P->d_tw, win, kmax, acc, what);
     const int h = n / 2 + 1;
     if (rs != h) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k");
     int B = 16;

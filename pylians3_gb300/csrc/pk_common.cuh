@@ -133,12 +133,12 @@ __device__ __forceinline__ void bin_mode_run(BinRun &R, Hist &H, const PkAcc &ac
     if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
 }
 
-// Eight consecutive modes kxx0 .. kxx0+7 of one pencil (ky, kz fixed), read
+// L consecutive modes kxx0 .. kxx0+L-1 of one pencil (ky, kz fixed), read
 // from shared memory at ln[pad(kxx)]: the same work as bin_mode_run, with the
 // bin index updated incrementally (n2 changes by 2 kx + 1 between neighbours)
 // instead of one square root per mode.
-template <int WHAT, class Hist, class Pad>
-__device__ __forceinline__ void bin_run8(Hist &H, const PkAcc &acc, const float2 *ln, Pad pad,
+template <int WHAT, int L, class Hist, class Pad>
+__device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 *ln, Pad pad,
                                          int kxx0, int ky, int kz, int n, int axis,
                                          const float *win, float wyz, int mid) {
     const bool even = (n & 1) == 0;
@@ -148,7 +148,7 @@ __device__ __forceinline__ void bin_run8(Hist &H, const PkAcc &acc, const float2
     int bin = isqrt_dev(kx0 * kx0 + r2);
     BinRun R;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < L; ++i) {
         const int kxx = kxx0 + i;
         const int kx = kxx > mid ? kxx - n : kxx;
         const int n2 = kx * kx + r2;

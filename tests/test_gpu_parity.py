@@ -182,8 +182,28 @@ def test_small_plain_config_vs_oracle(gpu, oracle, MAS, axis):
     assert pk_err(s.Pk, ref.Pk) <= TOL_PK
 
 
+@pytest.mark.parametrize("dims", [48, 96, 192])
+@pytest.mark.parametrize("MAS,axis", [("CIC", 0), ("PCS", 2)])
+def test_pk_3x2k_lengths_vs_oracle(gpu, oracle, dims, MAS, axis):
+    """Grids of 3 * 2^k cells take the radix-3 register FFT: Pk of the same
+    seeded overdensity and the fused particles path against the oracle."""
+    rng = np.random.default_rng(dims + 7)
+    pos = rng.random((4 * dims ** 3, 3), dtype=np.float32) * np.float32(BOX)
+    ref_d = np.zeros((dims,) * 3, np.float32)
+    oracle.MA(pos, ref_d, BOX, MAS)
+    ref_d /= np.mean(ref_d, dtype=np.float64)
+    ref_d -= 1.0
+    ref = oracle.Pk(ref_d, BOX, axis=axis, MAS=MAS, threads=8)
+    r = gpu.Pk_library.Pk(ref_d, BOX, axis=axis, MAS=MAS, verbose=False)
+    assert pk_err(r.Pk, ref.Pk) <= TOL_PK
+    assert np.array_equal(r.Nmodes3D, ref.Nmodes3D)
+    np.testing.assert_allclose(r.Pk1D, ref.Pk1D, rtol=TOL_PK, atol=TOL_PK * np.abs(ref.Pk1D).max())
+    s = gpu.power_spectrum(pos, dims, BOX, MAS, axis=axis)
+    assert pk_err(s.Pk, ref.Pk) <= TOL_PK
+
+
 # ------------------------------------------------------------------ FFTs
-@pytest.mark.parametrize("dims", [8, 16, 17, 24, 61, 64, 100, 128])
+@pytest.mark.parametrize("dims", [8, 16, 17, 24, 48, 61, 64, 96, 100, 128, 192, 384])
 def test_fft_r2c_c2r(gpu, dims):
     rng = np.random.default_rng(dims)
     a = rng.standard_normal((dims,) * 3).astype(np.float32)
