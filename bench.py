@@ -154,11 +154,15 @@ def stage_bytes(stage, dims, n, weighted):
     h = dims // 2 + 1
     real = 4 * dims ** 3
     half = 8 * dims * dims * h
+    rec = n * (12 + (4 if weighted else 0))   # one particle record (+ weight)
     return {
-        "deposit": n * (12 + (4 if weighted else 0)) + real,   # read particles, write grid once
-        "fft_z": real + half,                                   # read real grid, write half-complex
-        "fft_y": 2 * half,                                      # read + write
-        "pk_x": half,                                           # read only (spectrum not stored)
+        "tile_count": n * 12,        # read positions
+        "partition": 2 * rec,        # read + write every record once (a one-pass partition)
+        "deposit": rec + real,       # read the sorted records, write the grid once
+        "mass": n * 4 if weighted else 0,
+        "fft_z": real + half,        # read real grid, write half-complex
+        "fft_y": 2 * half,           # read + write
+        "pk_x": half,                # read only (spectrum not stored)
         "zero": real,
     }.get(stage)
 

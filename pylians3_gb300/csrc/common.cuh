@@ -62,9 +62,12 @@ struct PkAcc {
 }  // namespace pyl
 
 // Pipeline stages timed (on request) with CUDA events on the context stream.
+// The stages do not overlap: ST_BINS is the tile histogram and the scans of
+// the sorted deposit, ST_SORT its partition passes, ST_DEPOSIT the deposit
+// kernel proper, ST_MASS the total mass and FFT shift of the fused path.
 enum PylStage {
     ST_H2D = 0, ST_ZERO, ST_DEPOSIT, ST_SORT, ST_FFT_Z, ST_FFT_Y, ST_FFT_X, ST_PK_X,
-    ST_D2H, ST_COUNT
+    ST_D2H, ST_BINS, ST_MASS, ST_NSTAGES
 };
 
 // ------------------------------------------------------------------ context
@@ -79,8 +82,8 @@ struct pyl_ctx {
     struct Pending { int stage; cudaEvent_t a, b; };
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> event_pool;
-    double stage_ms[ST_COUNT] = {};
-    int64_t stage_n[ST_COUNT] = {};
+    double stage_ms[ST_NSTAGES] = {};
+    int64_t stage_n[ST_NSTAGES] = {};
 
     // The request issued by pyl_pk_particles_enqueue and not yet collected:
     // its raw sums are copied to `pinned` and `done` is recorded after them.

@@ -354,20 +354,21 @@ int pyl_ctx_stage_times(pyl_ctx *ctx, double *ms, int64_t *counts, int n, int re
     if (!ctx) return PYL_ERR_ARG;
     int st = stage_flush(ctx);
     if (st) return st;
-    for (int i = 0; i < n && i < ST_COUNT; ++i) {
+    for (int i = 0; i < n && i < ST_NSTAGES; ++i) {
         if (ms) ms[i] = ctx->stage_ms[i];
         if (counts) counts[i] = ctx->stage_n[i];
     }
     if (reset) {
-        for (int i = 0; i < ST_COUNT; ++i) { ctx->stage_ms[i] = 0.0; ctx->stage_n[i] = 0; }
+        for (int i = 0; i < ST_NSTAGES; ++i) { ctx->stage_ms[i] = 0.0; ctx->stage_n[i] = 0; }
     }
-    return ST_COUNT;
+    return ST_NSTAGES;
 }
 
 const char *pyl_stage_name(int stage) {
-    static const char *names[ST_COUNT] = {"h2d", "zero", "deposit", "sort", "fft_z",
-                                          "fft_y", "fft_x", "pk_x", "d2h"};
-    return (stage >= 0 && stage < ST_COUNT) ? names[stage] : "";
+    static const char *names[ST_NSTAGES] = {"h2d", "zero", "deposit", "partition", "fft_z",
+                                            "fft_y", "fft_x", "pk_x", "d2h", "tile_count",
+                                            "mass"};
+    return (stage >= 0 && stage < ST_NSTAGES) ? names[stage] : "";
 }
 
 int pyl_ctx_launch_count(const pyl_ctx *ctx, int64_t *count) {
@@ -575,6 +576,7 @@ int pk_device(pyl_ctx *ctx, const float *dgrid, int dims, int axis, int mas, int
     PYL_CUDA(ctx, cudaMemsetAsync(acc, 0, L.bytes(), ctx->stream));
     const PkAcc A = acc_view(acc, L);
     if (mi) {
+        StageScope s(ctx, ST_MASS);
         const double cells = (double)dims * dims * dims;
         if ((st = mass_and_shift(ctx, mi->W, mi->n, cells, A.mass, A.shift))) return st;
     }
@@ -753,11 +755,7 @@ int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const fl
         StageScope s(ctx, ST_ZERO);
         PYL_CUDA(ctx, cudaMemsetAsync(grid, 0, rb, ctx->stream));
     }
-    {
-        StageScope s(ctx, ST_DEPOSIT);
-        if ((st = deposit(ctx, dpos, n, 3, dW, grid, dims, BoxSize, mas_deposit, flags)))
-            return st;
-    }
+    if ((st = deposit(ctx, dpos, n, 3, dW, grid, dims, BoxSize, mas_deposit, flags))) return st;
     void *acc = nullptr;
     AccLayout L;
     const MassInfo mi{dW, n};

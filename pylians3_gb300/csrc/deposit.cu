@@ -115,6 +115,7 @@ int launch_atomic(pyl_ctx *ctx, const float *pos, long long n, int coord, const 
     long long blocks = (n + kThreads - 1) / kThreads;
     if (blocks > 152LL * 64) blocks = 152LL * 64;
     if (blocks < 1) blocks = 1;
+    StageScope s(ctx, ST_DEPOSIT);
     if (W)
         k_deposit_atomic<MAS, true, G><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(
             pos, n, coord, W, grid, dims, inv);
@@ -679,7 +680,7 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     {
-        StageScope s(ctx, ST_SORT);
+        StageScope s(ctx, ST_BINS);
         PYL_CUDA(ctx, cudaMemsetAsync(start, 0, sizeof(unsigned) * (size_t)(nt + 1), ctx->stream));
         PYL_CUDA(ctx, cudaMemsetAsync(flags2, 0, 2 * sizeof(unsigned), ctx->stream));
         const size_t hsm = sizeof(unsigned) * (size_t)nt;
@@ -699,6 +700,9 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         k_items<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(nchunk, start, nt, items, nitems);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
+    }
+    {
+        StageScope s(ctx, ST_SORT);
         // Both sorts are enqueued unless one is forced; each kernel reads the
         // mode chosen on the device and the other one returns at once.
         if (two_pass) {
@@ -732,6 +736,7 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
                                                                512, rsm));
     long long grid_n = (long long)(per_sm > 0 ? per_sm : 1) * sms * 4;
     if (grid_n > (long long)max_items) grid_n = (long long)max_items;
+    StageScope s(ctx, ST_DEPOSIT);
     k_tile_deposit<MAS, HAS_W><<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(
         b2, w2, start, items, nitems, inv, g, grid, vec4);
     ctx->launches++;
