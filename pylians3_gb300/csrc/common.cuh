@@ -100,6 +100,10 @@ struct pyl_ctx {
 
     struct Buf { void *p = nullptr; size_t bytes = 0; };
     std::map<std::string, Buf> ws;                       // named workspaces
+
+    // Status word the kernels set when a bounded wait gives up (bits of
+    // kStatusWaitTimeout, async_copy.cuh); read and cleared by status_check.
+    unsigned *d_status = nullptr;
 };
 
 namespace pyl {
@@ -112,6 +116,11 @@ int cuda_fail(pyl_ctx *ctx, cudaError_t e, const char *what);
         cudaError_t e_ = (call);                                             \
         if (e_ != cudaSuccess) return pyl::cuda_fail((ctx), e_, #call);      \
     } while (0)
+
+// Waits for the context stream, then reads and clears the device status
+// word: PYL_ERR_TIMEOUT if a kernel's bounded wait gave up since the last
+// check.
+int status_check(pyl_ctx *ctx);
 
 // Workspace of at least `bytes`, kept across calls under `name`.
 void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status);

@@ -29,6 +29,18 @@ int cuda_fail(pyl_ctx *ctx, cudaError_t e, const char *what) {
     return e == cudaErrorMemoryAllocation ? PYL_ERR_OOM : PYL_ERR_CUDA;
 }
 
+int status_check(pyl_ctx *ctx) {
+    unsigned s = 0;
+    PYL_CUDA(ctx, cudaMemcpyAsync(&s, ctx->d_status, sizeof s, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (s) {
+        PYL_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof s, ctx->stream));
+        return fail(ctx, PYL_ERR_TIMEOUT, "a device-side wait gave up (copy not completed)");
+    }
+    return PYL_OK;
+}
+
 void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status) {
     pyl_ctx::Buf &b = ctx->ws[name];
     if (b.bytes >= bytes && b.p) return b.p;
@@ -272,6 +284,15 @@ int pyl_ctx_create(pyl_ctx **out, int device, void *stream) {
         if (e != cudaSuccess) { delete ctx; return PYL_ERR_CUDA; }
         ctx->own_stream = true;
     }
+    e = cudaMalloc(&ctx->d_status, 16);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_status, 0, 16, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        if (ctx->d_status) cudaFree(ctx->d_status);
+        if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return PYL_ERR_CUDA;
+    }
     *out = ctx;
     return PYL_OK;
 }
@@ -293,6 +314,7 @@ int pyl_ctx_destroy(pyl_ctx *ctx) {
         cudaEventDestroy(p.a);
         if (p.b) cudaEventDestroy(p.b);
     }
+    if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PYL_OK;
@@ -320,8 +342,7 @@ int pyl_ctx_get_stream(const pyl_ctx *ctx, void **stream) {
 
 int pyl_synchronize(pyl_ctx *ctx) {
     if (!ctx) return PYL_ERR_ARG;
-    PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return PYL_OK;
+    return pyl::status_check(ctx);
 }
 
 const char *pyl_last_error(const pyl_ctx *ctx) {
@@ -442,7 +463,7 @@ static int ma_impl(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const f
     if (!dev) {
         PYL_CUDA(ctx, cudaMemcpyAsync(grid, dgrid, sizeof(G) * (size_t)cells,
                                       cudaMemcpyDeviceToHost, ctx->stream));
-        PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if ((st = status_check(ctx))) return st;
     }
     return PYL_OK;
 }
@@ -672,7 +693,8 @@ int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double
         PYL_CUDA(ctx, cudaMemcpyAsync(raw.data(), acc, sums + sizeof(float2) + sizeof(double),
                                       cudaMemcpyDeviceToHost, ctx->stream));
     }
-    PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int st = status_check(ctx);
+    if (st) return st;
     memcpy(dc, (const char *)raw.data() + sums, sizeof(float2));
     memcpy(mass, (const char *)raw.data() + sums + sizeof(float2), sizeof(double));
     return PYL_OK;
@@ -828,6 +850,7 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms) {
     int st = wait_done(ctx, timeout_ms);
     if (st) return st;   // a timeout leaves the request in flight
     ctx->req.active = false;
+    if ((st = status_check(ctx))) return st;
     const pyl_ctx::Request &R = ctx->req;
     const AccLayout &L = R.L;
     std::vector<double> raw(L.n3 + L.n1 + L.nph + L.n2 + 8);

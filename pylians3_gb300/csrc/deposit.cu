@@ -22,6 +22,9 @@
 // 2D (coord = 2) follows MA's expand_dims path: the third axis has extent 1,
 // index 0 and weight 1 for every tap, so a particle is deposited 2/3/4 times
 // onto the same plane for CIC/TSC/PCS (and renormalised by the caller).
+#include <algorithm>
+
+#include "async_copy.cuh"
 #include "deposit_common.cuh"
 
 namespace pyl {
@@ -258,6 +261,8 @@ __device__ __forceinline__ int tile_of(float x, float y, float z, float inv, con
 // coherent (e.g. a displaced lattice), and the single-pass frontier scatter
 // is then the cheaper sort.  A warp whose 32 particles share one tile adds
 // them with one shared atomic.
+constexpr int kCountUnroll = 4;
+
 template <int MAS>
 __global__ void __launch_bounds__(1024, 1)
 k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
@@ -269,22 +274,35 @@ k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
     __syncthreads();
     const int lane = threadIdx.x & 31;
     unsigned changes = 0;
-    for (long long b = (long long)blockIdx.x * blockDim.x; b < n;
-         b += (long long)gridDim.x * blockDim.x) {
-        const long long i = b + threadIdx.x;
-        const bool active = i < n;
-        const int t = active ? tile_of<MAS>(__ldg(pos + 3 * i), __ldg(pos + 3 * i + 1),
-                                            __ldg(pos + 3 * i + 2), inv, g)
-                             : -1;
-        const int prev = __shfl_up_sync(0xffffffffu, t, 1);
-        const int first = __shfl_sync(0xffffffffu, t, 0);
-        const bool same = __all_sync(0xffffffffu, t == first);
-        if (same) {
-            if (lane == 0 && t >= 0) atomicAdd(&s_cnt[t], 32u);
-            changes += (lane == 0) ? 1u : 0u;
-        } else if (active) {
-            atomicAdd(&s_cnt[t], 1u);
-            changes += (lane == 0 || t != prev) ? 1u : 0u;
+    // kCountUnroll rows of blockDim.x particles per iteration, all loads
+    // issued before any is used (the pass is bound by load latency)
+    const long long step = (long long)gridDim.x * blockDim.x * kCountUnroll;
+    for (long long b = (long long)blockIdx.x * blockDim.x * kCountUnroll; b < n; b += step) {
+        float x[kCountUnroll], y[kCountUnroll], z[kCountUnroll];
+#pragma unroll
+        for (int u = 0; u < kCountUnroll; ++u) {
+            const long long i = b + (long long)u * blockDim.x + threadIdx.x;
+            if (i < n) {
+                x[u] = __ldcs(pos + 3 * i);
+                y[u] = __ldcs(pos + 3 * i + 1);
+                z[u] = __ldcs(pos + 3 * i + 2);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kCountUnroll; ++u) {
+            const long long i = b + (long long)u * blockDim.x + threadIdx.x;
+            const bool active = i < n;
+            const int t = active ? tile_of<MAS>(x[u], y[u], z[u], inv, g) : -1;
+            const int prev = __shfl_up_sync(0xffffffffu, t, 1);
+            const int first = __shfl_sync(0xffffffffu, t, 0);
+            const bool same = __all_sync(0xffffffffu, t == first);
+            if (same) {
+                if (lane == 0 && t >= 0) atomicAdd(&s_cnt[t], 32u);
+                changes += (lane == 0 && t >= 0) ? 1u : 0u;
+            } else if (active) {
+                atomicAdd(&s_cnt[t], 1u);
+                changes += (lane == 0 || t != prev) ? 1u : 0u;
+            }
         }
     }
 #pragma unroll
@@ -332,21 +350,33 @@ __global__ void k_items(const unsigned *__restrict__ nchunk_ex, const unsigned *
 
 // One partition pass.  FINE = false: keys are coarse buckets (tile / F) of
 // the particles in input order; FINE = true: the input is grouped by coarse
-// bucket and each bucket is split into its F tiles.  A CTA owns an input
-// range of KP particles (split at coarse-bucket boundaries in the fine pass).
+// bucket and each bucket is split into its F tiles.
+//
+// Persistent CTAs walk the input in chunks of KP particles (chunk c, c +
+// gridDim.x, ...).  The next chunk is fetched into the other of two shared
+// buffers by a bulk copy (cp.async.bulk + mbarrier) while the current one is
+// partitioned, so the load latency is off the critical path.  Chunks that
+// are not whole or not 16-byte aligned (the tail; unaligned user pointers)
+// are read with plain loads.  A chunk is processed as segments that do not
+// straddle a coarse bucket (one segment in the coarse pass): keys, a shared
+// histogram, one global atomic per key on that key's cursor, a shared
+// counting sort, then each key's run is written out contiguously.
 template <int MAS, bool HAS_W, bool FINE>
 __global__ void __launch_bounds__(kPartThreads, 4)
 k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             float *__restrict__ dst, float *__restrict__ dstw, long long n, float inv,
             TileGeom g, unsigned *__restrict__ cursor, const unsigned *__restrict__ start,
-            const unsigned *__restrict__ mode) {
+            const unsigned *__restrict__ mode, int bulk, unsigned *__restrict__ status) {
     if (*mode != kSortTwoPass) return;   // the whole grid takes the same branch
-    extern __shared__ float sm[];
-    float *sp = sm;                    // 3*KP staged particles (input order)
-    float *sp2 = sp + 3 * KP;          // 3*KP particles in key order
-    float *sw = sp2 + 3 * KP;          // KP weights (input order)
-    float *sw2 = sw + (HAS_W ? KP : 0);
-    unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + (HAS_W ? KP : 0));
+    const long long nchunks = (n + KP - 1) / KP;
+    long long c = blockIdx.x;
+    if (c >= nchunks) return;
+    extern __shared__ __align__(16) float sm[];
+    constexpr int WS = HAS_W ? KP : 0;
+    // buffer b: positions at sm + 3*KP*b, weights at sm + 6*KP + WS*b
+    float *sp2 = sm + 6 * KP + 2 * WS;                   // 3*KP in key order
+    float *sw2 = sp2 + 3 * KP;
+    unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + WS);
     unsigned short *skey2 = skey + KP;
     unsigned *hist = reinterpret_cast<unsigned *>(skey2 + KP);   // kMaxKeys each
     unsigned *loff = hist + kMaxKeys;
@@ -354,83 +384,132 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
     unsigned *gbase = lcur + kMaxKeys;
     __shared__ unsigned s_warp[32];
     __shared__ long long s_seg[2];
+    __shared__ __align__(8) uint64_t s_bar[2];
 
-    const long long r0 = (long long)blockIdx.x * KP;
-    const long long r1 = min(n, r0 + KP);
-    long long seg0 = r0;
-    while (seg0 < r1) {
-        // ---- segment [seg0, seg1) with keys in [keybase, keybase + nkeys)
-        long long seg1 = r1;
-        int keybase = 0, nkeys = g.ncoarse;
-        if (FINE) {
-            if (threadIdx.x == 0) {
-                // coarse bucket containing position seg0: last c with start[c*F] <= seg0
-                int lo = 0, hi = g.ncoarse - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) / 2;
-                    if ((long long)start[min(mid * g.F, g.ntiles)] <= seg0) lo = mid;
-                    else hi = mid - 1;
+    auto whole = [&](long long cc) { return bulk && (cc + 1) * KP <= n; };
+    // thread 0: start the copy of chunk cc into buffer b
+    auto issue = [&](long long cc, int b) {
+        fence_proxy_async_smem();
+        const long long r0 = cc * KP;
+        mbar_arrive_expect_tx(&s_bar[b], (12u + (HAS_W ? 4u : 0u)) * KP);
+        bulk_copy_g2s(sm + 3 * KP * b, src + 3 * r0, 12u * KP, &s_bar[b]);
+        if (HAS_W) bulk_copy_g2s(sm + 6 * KP + WS * b, srcw + r0, 4u * KP, &s_bar[b]);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    unsigned parity = 0u;   // bit b: parity of the next phase of s_bar[b]
+    unsigned pend = 0u;     // bit b: a copy into buffer b is in flight
+    if (whole(c)) {
+        if (threadIdx.x == 0) issue(c, 0);
+        pend |= 1u;
+    }
+    int b = 0;
+    for (; c < nchunks; c += gridDim.x, b ^= 1) {
+        const long long cn = c + gridDim.x;
+        // buffer b^1 was released by the barrier that ended the last chunk
+        if (cn < nchunks && whole(cn)) {
+            if (threadIdx.x == 0) issue(cn, b ^ 1);
+            pend |= 2u >> b;   // bit b^1
+        }
+        const long long r0 = c * KP;
+        const int cnt = (int)min((long long)KP, n - r0);
+        float *sp = sm + 3 * KP * b;
+        float *sw = sm + 6 * KP + WS * b;
+        if (pend & (1u << b)) {
+            const unsigned ph = (parity >> b) & 1u;
+            const bool ok = mbar_wait_parity(&s_bar[b], ph);
+            parity ^= 1u << b;
+            pend &= ~(1u << b);
+            if (__syncthreads_or(!ok)) {
+                // a copy did not complete: record it, give each copy in
+                // flight one more bounded wait, and leave
+                if (threadIdx.x == 0) atomicOr(status, kStatusWaitTimeout);
+                mbar_wait_parity(&s_bar[b], ph);
+                if (pend) mbar_wait_parity(&s_bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+                return;
+            }
+        } else {
+            for (int j = threadIdx.x; j < 3 * cnt; j += blockDim.x) sp[j] = __ldcs(src + 3 * r0 + j);
+            if (HAS_W)
+                for (int j = threadIdx.x; j < cnt; j += blockDim.x) sw[j] = __ldcs(srcw + r0 + j);
+            __syncthreads();
+        }
+        const long long r1 = r0 + cnt;
+        long long seg0 = r0;
+        while (seg0 < r1) {
+            // ---- segment [seg0, seg1) with keys in [keybase, keybase + nkeys)
+            long long seg1 = r1;
+            int keybase = 0, nkeys = g.ncoarse;
+            if (FINE) {
+                if (threadIdx.x == 0) {
+                    // coarse bucket holding position seg0: last c with start[c*F] <= seg0
+                    int lo = 0, hi = g.ncoarse - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) / 2;
+                        if ((long long)start[min(mid * g.F, g.ntiles)] <= seg0) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    const long long bend = start[min((lo + 1) * g.F, g.ntiles)];
+                    s_seg[0] = lo;
+                    s_seg[1] = bend < r1 ? bend : r1;
                 }
-                const long long bend = start[min((lo + 1) * g.F, g.ntiles)];
-                s_seg[0] = lo;
-                s_seg[1] = bend < r1 ? bend : r1;
+                __syncthreads();
+                const int cb = (int)s_seg[0];
+                seg1 = s_seg[1];
+                keybase = cb * g.F;
+                nkeys = min(g.F, g.ntiles - keybase);
+            }
+            const int o = (int)(seg0 - r0);
+            const int cs = (int)(seg1 - seg0);
+            for (int k = threadIdx.x; k < nkeys; k += blockDim.x) hist[k] = 0u;
+            __syncthreads();
+            for (int i = threadIdx.x; i < cs; i += blockDim.x) {
+                const float *q = sp + 3 * (o + i);
+                const int t = tile_of<MAS>(q[0], q[1], q[2], inv, g);
+                const int key = FINE ? t - keybase : t / g.F;
+                skey[i] = (unsigned short)key;
+                atomicAdd(&hist[key], 1u);
             }
             __syncthreads();
-            const int c = (int)s_seg[0];
-            seg1 = s_seg[1];
-            keybase = c * g.F;
-            nkeys = min(g.F, g.ntiles - keybase);
-        }
-        const int cnt = (int)(seg1 - seg0);
-        for (int b = threadIdx.x; b < nkeys; b += blockDim.x) hist[b] = 0u;
-        __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const long long q = seg0 + i;
-            const float x = __ldcs(src + 3 * q), y = __ldcs(src + 3 * q + 1),
-                        z = __ldcs(src + 3 * q + 2);
-            const int t = tile_of<MAS>(x, y, z, inv, g);
-            const int key = FINE ? t - keybase : t / g.F;
-            sp[3 * i] = x;
-            sp[3 * i + 1] = y;
-            sp[3 * i + 2] = z;
-            if (HAS_W) sw[i] = __ldcs(srcw + q);
-            skey[i] = (unsigned short)key;
-            atomicAdd(&hist[key], 1u);
-        }
-        __syncthreads();
-        const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
-        const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
-        if (threadIdx.x < nkeys) {
-            loff[threadIdx.x] = ex;
-            lcur[threadIdx.x] = ex;
-            gbase[threadIdx.x] = hv ? atomicAdd(&cursor[keybase + threadIdx.x], hv) : 0u;
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const int key = skey[i];
-            const unsigned r = atomicAdd(&lcur[key], 1u);
-            sp2[3 * r] = sp[3 * i];
-            sp2[3 * r + 1] = sp[3 * i + 1];
-            sp2[3 * r + 2] = sp[3 * i + 2];
-            if (HAS_W) sw2[r] = sw[i];
-            skey2[r] = (unsigned short)key;
-        }
-        __syncthreads();
-        // key runs are contiguous both here and in the destination
-        for (int j = threadIdx.x; j < 3 * cnt; j += blockDim.x) {
-            const int e = j / 3;
-            const int key = skey2[e];
-            const size_t d = (size_t)gbase[key] + (e - loff[key]);
-            dst[3 * d + (j - 3 * e)] = sp2[j];
-        }
-        if (HAS_W) {
-            for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-                const int key = skey2[e];
-                dstw[(size_t)gbase[key] + (e - loff[key])] = sw2[e];
+            const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
+            const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
+            if (threadIdx.x < nkeys) {
+                loff[threadIdx.x] = ex;
+                lcur[threadIdx.x] = ex;
+                gbase[threadIdx.x] = hv ? atomicAdd(&cursor[keybase + threadIdx.x], hv) : 0u;
             }
+            __syncthreads();
+            for (int i = threadIdx.x; i < cs; i += blockDim.x) {
+                const int key = skey[i];
+                const unsigned r = atomicAdd(&lcur[key], 1u);
+                const float *q = sp + 3 * (o + i);
+                sp2[3 * r] = q[0];
+                sp2[3 * r + 1] = q[1];
+                sp2[3 * r + 2] = q[2];
+                if (HAS_W) sw2[r] = sw[o + i];
+                skey2[r] = (unsigned short)key;
+            }
+            __syncthreads();
+            // key runs are contiguous both here and in the destination
+            for (int j = threadIdx.x; j < 3 * cs; j += blockDim.x) {
+                const int e = j / 3;
+                const int key = skey2[e];
+                const size_t d = (size_t)gbase[key] + (e - loff[key]);
+                dst[3 * d + (j - 3 * e)] = sp2[j];
+            }
+            if (HAS_W) {
+                for (int e = threadIdx.x; e < cs; e += blockDim.x) {
+                    const int key = skey2[e];
+                    dstw[(size_t)gbase[key] + (e - loff[key])] = sw2[e];
+                }
+            }
+            __syncthreads();
+            seg0 = seg1;
         }
-        __syncthreads();
-        seg0 = seg1;
     }
 }
 
@@ -475,17 +554,65 @@ __device__ __forceinline__ void red_v4(float *addr, float a, float b, float c, f
                  :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
 }
 
+// Largest weight of one tap (product of the three axis weights) per scheme.
+template <int MAS>
+struct TapBound {
+    static constexpr float WMAX = MAS == PYL_MAS_TSC ? 0.421875f          // 0.75^3
+                                : MAS == PYL_MAS_PCS ? 0.2962963f         // (2/3)^3
+                                                     : 1.0f;
+};
+
+// In place along one line of n ints (stride st):
+//     a[j] <- sum of a[k] for k in [j - HI, j + LO]   (0 outside the line),
+// the cells whose taps can reach cell j (taps lie at home + [-LO, HI]).
+// The last LO + HI inputs are kept in registers while the line is rewritten.
+template <int LO, int HI>
+__device__ __forceinline__ int box_line(int *a, int n, int st, bool write) {
+    constexpr int R = LO + HI + 1;
+    int r[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) r[q] = 0;
+    int sum = 0, best = 0;
+    for (int k = 0; k < n + LO; ++k) {
+        const int x = k < n ? a[k * st] : 0;
+        sum += x - r[0];
+#pragma unroll
+        for (int q = 0; q + 1 < R; ++q) r[q] = r[q + 1];
+        r[R - 1] = x;
+        const int j = k - LO;
+        if (j >= 0) {
+            if (write) a[j * st] = sum;
+            best = max(best, sum);
+        }
+    }
+    return best;
+}
+
 // Deposit: work items (tile, chunk) over a persistent grid; shared
 // footprint, shared atomics, then a global flush of the footprint.
-template <int MAS, bool HAS_W>
+//
+// FIXED (unit weights): the footprint is accumulated in 32-bit integers,
+// each tap rounded to a fixed point of scale 2^e.  A first pass over the
+// item's particles histograms their home cells; a box sum of the histogram
+// over the stencil's reach gives, for every footprint cell, how many
+// particles can reach it, so no cell can exceed WMAX times the largest box
+// sum, and 2^e is the largest power of two keeping that bound under 2^30.
+// Integer shared atomics run at about twice the rate of float ones, and the
+// sums are exact (independent of the order of the atomics); the flush
+// converts each cell once (int -> float rounding, then an exact scaling by
+// 2^-e).
+template <int MAS, bool HAS_W, bool FIXED>
 __global__ void __launch_bounds__(512)
 k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                const unsigned *__restrict__ start, const uint2 *__restrict__ items,
                const unsigned *__restrict__ nitems, float inv, TileGeom g,
                float *__restrict__ grid, int vec4) {
+    static_assert(!(FIXED && HAS_W), "fixed-point accumulation is for unit weights");
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
     extern __shared__ float s_reg[];
+    int *s_int = reinterpret_cast<int *>(s_reg);
+    __shared__ int s_max[32];
     const int RX = g.RX, RY = g.RY, RZ = g.RZ;
     const int cells = RX * RY * RZ;
     const unsigned total = *nitems;
@@ -498,6 +625,47 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         const long long p0 = (long long)start[t] + (long long)item.y * kItemCap;
         const long long p1 = min((long long)start[t + 1], p0 + (long long)kItemCap);
         __syncthreads();
+        float scale = 1.f, inv_scale = 1.f;
+        if (FIXED) {
+            // ---- home-cell occupancy of the item, its maximum, the scale
+            for (long long i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+                const int hx = wrap_idx(home_cell<MAS>(cell_dist(__ldg(spos + 3 * i), inv)), g.dims);
+                const int hy =
+                    wrap_idx(home_cell<MAS>(cell_dist(__ldg(spos + 3 * i + 1), inv)), g.dims);
+                const int hz =
+                    wrap_idx(home_cell<MAS>(cell_dist(__ldg(spos + 3 * i + 2), inv)), g.dims);
+                atomicAdd(&s_int[((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ +
+                                 (hz - oz + S::LO)],
+                          1);
+            }
+            __syncthreads();
+            // separable box sums: z lines, y lines, then x lines (max only)
+            for (int l = threadIdx.x; l < RX * RY; l += blockDim.x)
+                box_line<S::LO, S::HI>(s_int + l * RZ, RZ, 1, true);
+            __syncthreads();
+            for (int l = threadIdx.x; l < RX * RZ; l += blockDim.x)
+                box_line<S::LO, S::HI>(s_int + (l / RZ) * RY * RZ + (l % RZ), RY, RZ, true);
+            __syncthreads();
+            int m = 0;
+            for (int l = threadIdx.x; l < RY * RZ; l += blockDim.x)
+                m = max(m, box_line<S::LO, S::HI>(s_int + l, RX, RY * RZ, false));
+            __syncthreads();
+            for (int i = threadIdx.x; i < cells; i += blockDim.x) s_int[i] = 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+            __syncthreads();
+            m = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = max(m, s_max[w]);
+            // 2^e <= 2^30 / (WMAX * largest box sum)
+            const float bound = fmaxf(TapBound<MAS>::WMAX * (float)m, 1.f);
+            int e;
+            frexpf(bound, &e);                 // bound < 2^e
+            e = min(30 - e, 30);
+            scale = ldexpf(1.f, e);
+            inv_scale = ldexpf(1.f, -e);
+            __syncthreads();   // s_max is rewritten by the next item
+        }
         for (long long i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
             int lx[NT], ly[NT], lz[NT];
             float wx[NT], wy[NT], wz[NT];
@@ -534,17 +702,22 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
 #pragma unroll
                 for (int m = 0; m < NT; ++m) {
                     const float wxy = wx[l] * wy[m];
-                    float *row = s_reg + (lx[l] * RY + ly[m]) * RZ;
+                    const int row = (lx[l] * RY + ly[m]) * RZ;
 #pragma unroll
                     for (int q = 0; q < NT; ++q) {
                         float v = wxy * wz[q];
                         if (HAS_W) v *= wt;
-                        atomicAdd(row + lz[q], v);
+                        if (FIXED) atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
+                        else atomicAdd(s_reg + row + lz[q], v);
                     }
                 }
             }
         }
         __syncthreads();
+        // footprint cell value as a float
+        auto cell = [&](int c) {
+            return FIXED ? (float)s_int[c] * inv_scale : s_reg[c];
+        };
         const int d = g.dims;
         const long long dd = (long long)d * d;
         const int zs = oz - S::LO;  // unwrapped global z of footprint column 0
@@ -563,7 +736,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int lz = zq + e - zs;
-                    v[e] = (lz >= 0 && lz < RZ) ? s_reg[(lx * RY + ly) * RZ + lz] : 0.f;
+                    v[e] = (lz >= 0 && lz < RZ) ? cell((lx * RY + ly) * RZ + lz) : 0.f;
                 }
                 if (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f) {
                     const int gx = wrap_idx(ox - S::LO + lx, d);
@@ -574,7 +747,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             }
         } else {
             for (int c = threadIdx.x; c < cells; c += blockDim.x) {
-                const float v = s_reg[c];
+                const float v = cell(c);
                 if (v == 0.f) continue;
                 const int lz = c % RZ, ly = (c / RZ) % RY, lx = c / (RZ * RY);
                 const int gx = wrap_idx(ox - S::LO + lx, d);
@@ -634,14 +807,15 @@ TileGeom make_geom(int dims, int mas) {
     return g;
 }
 
+// two input buffers, the key-ordered buffer, keys and per-key tables
 size_t partition_smem(bool weighted) {
-    return sizeof(float) * (6 * (size_t)KP + (weighted ? 2 * (size_t)KP : 0)) +
+    return sizeof(float) * (9 * (size_t)KP + (weighted ? 3 * (size_t)KP : 0)) +
            sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 4 * kMaxKeys;
 }
 
 template <int MAS, bool HAS_W>
 int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
-                    int dims, float inv, const TileGeom &g, int forced_mode) {
+                    int dims, float inv, const TileGeom &g, int forced_mode, bool fixed) {
     int st = PYL_OK;
     const int nt = g.ntiles;
     const bool two_pass = forced_mode != kSortFrontier;   // may be chosen on the device
@@ -707,15 +881,24 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         // mode chosen on the device and the other one returns at once.
         if (two_pass) {
             const size_t psm = partition_smem(HAS_W);
-            const long long nblk = (n + KP - 1) / KP;
             if ((st = set_smem(ctx, k_partition<MAS, HAS_W, false>, psm))) return st;
-            k_partition<MAS, HAS_W, false><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
-                pos, W, b1, w1, n, inv, g, ccur, start, mode);
+            if ((st = set_smem(ctx, k_partition<MAS, HAS_W, true>, psm))) return st;
+            static int per_sm = 0;   // resident partition CTAs per SM (same for both passes)
+            if (!per_sm) {
+                PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                  &per_sm, k_partition<MAS, HAS_W, true>, kPartThreads, psm));
+                if (per_sm < 1) per_sm = 1;
+            }
+            const long long nchunks = (n + KP - 1) / KP;
+            const unsigned nblk = (unsigned)std::min<long long>(nchunks, (long long)per_sm * sms);
+            // bulk copies need 16-byte aligned sources (the workspaces are)
+            const int bulk_in = ((uintptr_t)pos & 15) == 0 && (!W || ((uintptr_t)W & 15) == 0);
+            k_partition<MAS, HAS_W, false><<<nblk, kPartThreads, psm, ctx->stream>>>(
+                pos, W, b1, w1, n, inv, g, ccur, start, mode, bulk_in, ctx->d_status);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
-            if ((st = set_smem(ctx, k_partition<MAS, HAS_W, true>, psm))) return st;
-            k_partition<MAS, HAS_W, true><<<(unsigned)nblk, kPartThreads, psm, ctx->stream>>>(
-                b1, w1, b2, w2, n, inv, g, fcur, start, mode);
+            k_partition<MAS, HAS_W, true><<<nblk, kPartThreads, psm, ctx->stream>>>(
+                b1, w1, b2, w2, n, inv, g, fcur, start, mode, 1, ctx->d_status);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
         }
@@ -730,18 +913,24 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
     }
     const int vec4 = (dims % 4 == 0 && ((uintptr_t)grid & 15) == 0) ? 1 : 0;
     const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
-    if ((st = set_smem(ctx, k_tile_deposit<MAS, HAS_W>, rsm))) return st;
-    int per_sm = 0;
-    PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_deposit<MAS, HAS_W>,
-                                                               512, rsm));
-    long long grid_n = (long long)(per_sm > 0 ? per_sm : 1) * sms * 4;
-    if (grid_n > (long long)max_items) grid_n = (long long)max_items;
-    StageScope s(ctx, ST_DEPOSIT);
-    k_tile_deposit<MAS, HAS_W><<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(
-        b2, w2, start, items, nitems, inv, g, grid, vec4);
-    ctx->launches++;
-    PYL_CUDA(ctx, cudaGetLastError());
-    return PYL_OK;
+    auto run = [&](auto kernel) -> int {
+        int st2;
+        if ((st2 = set_smem(ctx, kernel, rsm))) return st2;
+        int per_sm = 0;
+        PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 512, rsm));
+        long long grid_n = (long long)(per_sm > 0 ? per_sm : 1) * sms * 4;
+        if (grid_n > (long long)max_items) grid_n = (long long)max_items;
+        StageScope s(ctx, ST_DEPOSIT);
+        kernel<<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(b2, w2, start, items, nitems, inv, g,
+                                                           grid, vec4);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+        return PYL_OK;
+    };
+    if constexpr (!HAS_W) {
+        if (fixed) return run(k_tile_deposit<MAS, false, true>);
+    }
+    return run(k_tile_deposit<MAS, HAS_W, false>);
 }
 
 template <int MAS>
@@ -750,8 +939,10 @@ int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, f
     const TileGeom g = make_geom(dims, MAS);
     const int forced = (flags & PYL_SORT_TWO_PASS) ? kSortTwoPass
                        : (flags & PYL_SORT_FRONTIER) ? kSortFrontier : -1;
-    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced)
-             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced);
+    // unit weights accumulate in fixed point unless float atomics are asked for
+    const bool fixed = !(flags & PYL_DEPOSIT_FLOAT);
+    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced, false)
+             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced, fixed);
 }
 
 bool use_sorted(long long n, int coord, int dims, int mas, int flags) {

@@ -1,7 +1,8 @@
-"""Both deposit paths (unsorted global atomics and tile-sorted shared memory),
-forced through the C ABI flags, against the oracle on uniform, clustered and
-edge-case inputs.  Grids agree to float32 rounding of a different summation
-order: |diff| <= 1e-5 * max(1, |value|)."""
+"""Both deposit paths (unsorted global atomics and tile-sorted shared memory,
+the latter with fixed-point or float32 shared accumulation), forced through
+the C ABI flags, against the oracle on uniform, clustered and edge-case
+inputs.  Grids agree to float32 rounding of a different summation order (or
+the fixed point's rounding of each tap): |diff| <= 1e-5 * max(1, |value|)."""
 import ctypes
 
 import numpy as np
@@ -57,13 +58,22 @@ def test_paths_match_oracle(native, oracle, dims, MAS, kind):
     for w in (None, W):
         ref = np.zeros((dims,) * 3, np.float32)
         oracle.MA(pos, ref, BOX, MAS, W=w)
+        # Dense clustered cells sum ~1e4 float32 terms: the oracle's own
+        # rounding (vs its float64 deposit) can exceed 1e-5 of the maximum.
+        # Every path must be as close to the float64 grid as 3x that, or
+        # within 1e-5 of the maximum of the float32 oracle.
+        ref64 = oracle.MA_f64(pos, dims, BOX, MAS, W=w)
+        own = float(np.abs(ref - ref64).max())
         tol = 1e-5 * max(1.0, float(np.abs(ref).max()))
         for flags in (native.PYL_DEPOSIT_SORTED,
                       native.PYL_DEPOSIT_SORTED | native.PYL_SORT_TWO_PASS,
                       native.PYL_DEPOSIT_SORTED | native.PYL_SORT_FRONTIER,
+                      native.PYL_DEPOSIT_SORTED | native.PYL_DEPOSIT_FLOAT,
                       native.PYL_DEPOSIT_ATOMIC):
             g = run_ma(native, pos, dims, MAS, w, flags)
-            assert float(np.abs(g - ref).max()) <= tol, (flags, w is None)
+            ok = (float(np.abs(g - ref).max()) <= tol or
+                  float(np.abs(g - ref64).max()) <= 3 * own)
+            assert ok, (flags, w is None, float(np.abs(g - ref).max()), own)
 
 
 def test_sorted_accumulates(native, oracle):
