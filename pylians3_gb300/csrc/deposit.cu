@@ -628,15 +628,27 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         float scale = 1.f, inv_scale = 1.f;
         if (FIXED) {
             // ---- home-cell occupancy of the item, its maximum, the scale
-            for (long long i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
-                const int hx = wrap_idx(home_cell<MAS>(cell_dist(__ldg(spos + 3 * i), inv)), g.dims);
-                const int hy =
-                    wrap_idx(home_cell<MAS>(cell_dist(__ldg(spos + 3 * i + 1), inv)), g.dims);
-                const int hz =
-                    wrap_idx(home_cell<MAS>(cell_dist(__ldg(spos + 3 * i + 2), inv)), g.dims);
+            auto occupy = [&](float x, float y, float z) {
+                const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
+                const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
+                const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
                 atomicAdd(&s_int[((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ +
                                  (hz - oz + S::LO)],
                           1);
+            };
+            // two particles per thread and step, both loaded first
+            for (long long i = p0 + threadIdx.x; i < p1; i += 2 * blockDim.x) {
+                const long long i2 = i + blockDim.x;
+                const float x = __ldg(spos + 3 * i), y = __ldg(spos + 3 * i + 1),
+                            z = __ldg(spos + 3 * i + 2);
+                float x2 = 0.f, y2 = 0.f, z2 = 0.f;
+                if (i2 < p1) {
+                    x2 = __ldg(spos + 3 * i2);
+                    y2 = __ldg(spos + 3 * i2 + 1);
+                    z2 = __ldg(spos + 3 * i2 + 2);
+                }
+                occupy(x, y, z);
+                if (i2 < p1) occupy(x2, y2, z2);
             }
             __syncthreads();
             // separable box sums: z lines, y lines, then x lines (max only)
@@ -666,11 +678,11 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             inv_scale = ldexpf(1.f, -e);
             __syncthreads();   // s_max is rewritten by the next item
         }
-        for (long long i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+        auto deposit_one = [&](float px, float py, float pz, float wt) {
             int lx[NT], ly[NT], lz[NT];
             float wx[NT], wy[NT], wz[NT];
             {
-                const float d = cell_dist(__ldcs(spos + 3 * i + 0), inv);
+                const float d = cell_dist(px, inv);
                 const int c = home_cell<MAS>(d);
                 const int base = wrap_idx(c, g.dims) - ox + S::LO;
                 int o[NT];
@@ -679,7 +691,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 for (int j = 0; j < NT; ++j) lx[j] = base + o[j];
             }
             {
-                const float d = cell_dist(__ldcs(spos + 3 * i + 1), inv);
+                const float d = cell_dist(py, inv);
                 const int c = home_cell<MAS>(d);
                 const int base = wrap_idx(c, g.dims) - oy + S::LO;
                 int o[NT];
@@ -688,7 +700,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 for (int j = 0; j < NT; ++j) ly[j] = base + o[j];
             }
             {
-                const float d = cell_dist(__ldcs(spos + 3 * i + 2), inv);
+                const float d = cell_dist(pz, inv);
                 const int c = home_cell<MAS>(d);
                 const int base = wrap_idx(c, g.dims) - oz + S::LO;
                 int o[NT];
@@ -696,7 +708,6 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
 #pragma unroll
                 for (int j = 0; j < NT; ++j) lz[j] = base + o[j];
             }
-            const float wt = HAS_W ? __ldcs(sw + i) : 1.f;
 #pragma unroll
             for (int l = 0; l < NT; ++l) {
 #pragma unroll
@@ -712,6 +723,22 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                     }
                 }
             }
+        };
+        // two particles per thread and step, both loaded first
+        for (long long i = p0 + threadIdx.x; i < p1; i += 2 * blockDim.x) {
+            const long long i2 = i + blockDim.x;
+            const float x = __ldcs(spos + 3 * i), y = __ldcs(spos + 3 * i + 1),
+                        z = __ldcs(spos + 3 * i + 2);
+            const float w = HAS_W ? __ldcs(sw + i) : 1.f;
+            float x2 = 0.f, y2 = 0.f, z2 = 0.f, w2 = 1.f;
+            if (i2 < p1) {
+                x2 = __ldcs(spos + 3 * i2);
+                y2 = __ldcs(spos + 3 * i2 + 1);
+                z2 = __ldcs(spos + 3 * i2 + 2);
+                if (HAS_W) w2 = __ldcs(sw + i2);
+            }
+            deposit_one(x, y, z, w);
+            if (i2 < p1) deposit_one(x2, y2, z2, w2);
         }
         __syncthreads();
         // footprint cell value as a float
@@ -762,7 +789,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
 
 template <typename K>
 int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
-    if (bytes > 48 * 1024)
+    if (bytes > 40 * 1024)   // static shared memory counts toward the 48 KB default too
         PYL_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)bytes));
     return PYL_OK;

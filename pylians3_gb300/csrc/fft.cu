@@ -119,7 +119,7 @@ k_axis_c2c(float2 *__restrict__ data, int h, int axis, FftDesc D,
 
 template <typename K>
 int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
-    if (bytes > 48 * 1024)
+    if (bytes > 40 * 1024)   // static shared memory counts toward the 48 KB default too
         PYL_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)bytes));
     return PYL_OK;

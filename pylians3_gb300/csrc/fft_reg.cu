@@ -151,8 +151,8 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
     float2 *line = sm + N + c * LINE;
     float *win = reinterpret_cast<float *>(sm + N + C * LINE);
     FltHist H;
-    H.setup(win + N, kmax, MID, WHAT);
-    for (int i = threadIdx.x; i < N; i += blockDim.x) { tw[i] = g_tw[i]; win[i] = g_win[i]; }
+    H.setup(win + RegPlan<N>::LINE, kmax, MID, WHAT);   // window padded like the lines
+    for (int i = threadIdx.x; i < N; i += blockDim.x) { tw[i] = g_tw[i]; win[pad8(i)] = g_win[i]; }
     H.zero_all();
     __syncthreads();
     const int nzb = (h + C - 1) / C;
@@ -186,7 +186,7 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
             if (kzc < h) {
                 const float2 *ln = sm + N + cc * LINE;
                 const int ky = kyy > MID ? kyy - N : kyy;
-                const float wyz = win[kyy] * win[kzc];
+                const float wyz = win[pad8(kyy)] * win[pad8(kzc)];
                 constexpr int E = RegPlan<N>::E;
                 bin_run<WHAT, E>(H, acc, ln, [](int i) { return pad8(i); }, E * rr, ky, kzc, N,
                                  axis, win, wyz, MID);
@@ -199,7 +199,7 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
 
 template <typename K>
 int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
-    if (bytes > 48 * 1024)
+    if (bytes > 40 * 1024)   // static shared memory counts toward the 48 KB default too
         PYL_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)bytes));
     return PYL_OK;
@@ -261,7 +261,7 @@ int pk_n(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const float2
          const float *win, int kmax, const PkAcc &acc) {
     using CF = ColsCfg<N>;
     const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE) +
-                        sizeof(float) * N + FltHist::bytes(kmax, N / 2, WHAT);
+                        sizeof(float) * RegPlan<N>::LINE + FltHist::bytes(kmax, N / 2, WHAT);
     if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "Pk histogram too large");
     int st;
     if ((st = set_smem(ctx, k_pk_x_p2<N, WHAT>, smem))) return st;

@@ -134,7 +134,9 @@ __device__ __forceinline__ void bin_mode_run(BinRun &R, Hist &H, const PkAcc &ac
 }
 
 // L consecutive modes kxx0 .. kxx0+L-1 of one pencil (ky, kz fixed), read
-// from shared memory at ln[pad(kxx)]: the same work as bin_mode_run, with the
+// from shared memory at ln[pad(kxx)], the window at win[pad(kxx)] (the pad
+// spreads the L-strided accesses of a warp over the banks): the same work as
+// bin_mode_run, with the
 // bin index updated incrementally (n2 changes by 2 kx + 1 between neighbours)
 // instead of one square root per mode.
 template <int WHAT, int L, class Hist, class Pad>
@@ -161,7 +163,7 @@ __device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 
         const float2 v = ln[pad(kxx)];
         if (n2 == 0) *acc.dc = v;
         const int kpar = axis == 0 ? kx : (axis == 1 ? ky : kz);
-        const float f = win[kxx] * wyz;
+        const float f = win[pad(kxx)] * wyz;
         const float re = v.x * f, im = v.y * f;
         const float d2 = re * re + im * im;
         const float mu2 = n2 > 0 ? (float)(kpar * kpar) * __frcp_rn((float)n2) : 0.f;
