@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="plain", choices=["plain", "batched", "served"],
+    ap.add_argument("--mode", default="plain",
+                    choices=["plain", "batched", "served", "precision"],
                     help="plain: the headline line; batched: 64 uneven realizations "
                          "overlapped; served: Poisson request streams")
     ap.add_argument("--slots", type=int, default=8)
@@ -61,6 +62,8 @@ def parse():
                     help="tile sort of the deposit: chosen on the device from the input "
                          "order (auto), one pass with per-tile cursors, or two staged "
                          "partition passes")
+    ap.add_argument("--halos", type=float, default=0.1,
+                    help="precision mode: extra fraction of particles in Plummer halos")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16,
@@ -512,10 +515,92 @@ def run_served(a):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- precision
+def run_precision(a):
+    """Accuracy of the float32 pipeline variants against the float64 oracle
+    on the precision workload: a Zel'dovich lattice (sigma 3 Mpc/h, RSD) on
+    dims^3 plus 10% extra particles in 1000 Plummer halos (scale 0.5 Mpc/h),
+    deposited with a.mas.  Variants: the default deposit (fixed-point tiles),
+    float32 shared atomics, the compensated deposit, and a float64 GPU grid
+    (pyl_ma_f64) through the float32 FFT and binning (isolates the FFT).
+    The oracle: float64 deposit on all host cores, float64 FFT, float64
+    binning.  Per bin, err = max over ell of |P_ell - P_ell^64| / |P_0^64|."""
+    import numpy as np
+    import torch
+    from pylians3_gb300 import build_native
+    build_native.build()
+    import pylians3_gb300 as P
+    from pylians3_gb300 import synth
+    from oracle import oracle as orc
+    dims = a.dims
+    lattice = synth.zeldovich(dims, BOX, sigma=3.0, seed=2027)
+    nh = int(lattice.shape[0] * a.halos)
+    if nh:
+        halos = synth.plummer_halos(nh, 1000, 0.5, BOX, seed=2028)
+        pos = torch.cat([lattice, halos])
+        del halos
+    else:
+        pos = lattice
+    del lattice
+    n = int(pos.shape[0])
+    torch.cuda.synchronize()
+    spectra, secs = {}, {}
+    for name, dep in (("fixed_point_tiles", "auto"), ("float32_atomics", "float"),
+                      ("compensated", "compensated")):
+        P.power_spectrum(pos, dims, BOX, a.mas, axis=a.axis, deposit=dep)   # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        spectra[name] = P.power_spectrum(pos, dims, BOX, a.mas, axis=a.axis, deposit=dep).Pk
+        secs[name] = time.perf_counter() - t0
+    g64 = torch.zeros((dims,) * 3, dtype=torch.float64, device="cuda")
+    P.MAS_library._deposit(pos, g64, BOX, a.mas, None, 3, True, "float64")
+    d = (g64 / g64.mean() - 1.0).to(torch.float32)
+    del g64
+    spectra["float64_grid_float32_fft"] = P.Pk_library.Pk(d, BOX, axis=a.axis, MAS=a.mas,
+                                                         verbose=False).Pk
+    del d
+    pos_np = pos.cpu().numpy()
+    del pos
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    threads = os.cpu_count() or 1
+    grid = orc.MA_f64(pos_np, dims, BOX, a.mas, threads=0)
+    del pos_np
+    grid /= grid.mean()
+    grid -= 1.0
+    ref = orc.Pk_f64(grid, BOX, axis=a.axis, MAS=a.mas, threads=threads)
+    t_oracle = time.perf_counter() - t0
+    del grid
+    mid = dims // 2
+    rows = {}
+    for name, pk in spectra.items():
+        err = np.abs(pk - ref.Pk).max(axis=1) / np.abs(ref.Pk[:, 0])
+        rows[name] = {
+            "max_err_k_le_nyquist": float(err[:mid].max()),
+            "median_err_k_le_nyquist": float(np.median(err[:mid])),
+            "max_err_all_bins": float(err.max()),
+            "bins_over_1e-4": int((err > 1e-4).sum()),
+            "seconds": secs.get(name)}
+        np.save(os.path.join(ROOT, "gpurun_out", "precision_err_%s_%s_%d_h%g.npy"
+                             % (name, a.mas, dims, a.halos)), err)
+    line = {"mode": "precision", "metric": "per-bin error of P_ell vs the float64 oracle",
+            "unit": "max over ell |dP_ell| / |P_0|, per bin", "bins": int(len(ref.Pk)),
+            "nyquist_bin": mid, "variants": rows, "oracle_seconds": t_oracle,
+            "config": {"workload": "%d^3 Zel'dovich lattice (sigma 3 Mpc/h, RSD) + %g%% in 1000 "
+                                   "Plummer halos (a = 0.5 Mpc/h), %s deposit + window, axis %d"
+                                   % (dims, 100 * a.halos, a.mas, a.axis),
+                       "particles": n, "dims": dims, "mas": a.mas, "axis": a.axis,
+                       "oracle": "float64 deposit (all host cores), float64 FFT, float64 sums"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.mode == "precision":
+        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+        run_precision(a)
     elif a.mode == "batched":
         run_batched(a)
     elif a.mode == "served":

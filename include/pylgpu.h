@@ -57,10 +57,11 @@ enum { PYL_MAS_NONE = 0, PYL_MAS_NGP = 1, PYL_MAS_CIC = 2, PYL_MAS_TSC = 3,
  * otherwise; these flags force one of them.                                */
 #define PYL_SORT_TWO_PASS  0x10
 #define PYL_SORT_FRONTIER  0x20
-/* The tile-sorted deposit of unit-weight particles accumulates each tile in
- * 32-bit fixed point: each tap is rounded once to a scale chosen per tile
- * from its densest cell (so that no cell can overflow), and the tile's sums
- * are then exact.  This flag keeps float32 shared atomics instead.         */
+/* The tile-sorted NGP/CIC/TSC deposit of unit-weight particles accumulates
+ * each tile in 32-bit fixed point: each tap is rounded once to a scale
+ * chosen per tile from its densest region (so that no cell can overflow),
+ * and the tile's sums are then exact.  This flag keeps float32 shared
+ * atomics instead (always used for PCS and for weighted particles).        */
 #define PYL_DEPOSIT_FLOAT  0x40
 
 /* Which Pk outputs to compute (bit mask); the 3D multipoles always are.   */

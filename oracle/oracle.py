@@ -72,6 +72,8 @@ def _load():
     lib.orc_deposit_omp.argtypes = [ctypes.c_int, fp, ctypes.c_long, fp, fp,
                                     ctypes.c_int, ctypes.c_float, ctypes.c_int]
     lib.orc_deposit_omp.restype = None
+    lib.orc_deposit_d_omp.argtypes = lib.orc_deposit_omp.argtypes
+    lib.orc_deposit_d_omp.restype = None
     lib.orc_pk_bin.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, ctypes.c_int] + [fp] * 9
     lib.orc_pk_bin.restype = None
@@ -125,10 +127,20 @@ def MA(pos, number, BoxSize, MAS="CIC", W=None, verbose=False,
             number2 /= {"CIC": 2.0, "TSC": 3.0, "PCS": 4.0}[MAS]
 
 
-def MA_f64(pos, dims, BoxSize, MAS="CIC", W=None):
+def MA_f64(pos, dims, BoxSize, MAS="CIC", W=None, threads=1):
     """Float64 grid deposit (precision oracle); weights computed as the
-    reference computes them, accumulation in float64 (cf. CICW_d :229-266)."""
+    reference computes them, accumulation in float64 (cf. CICW_d :229-266).
+    threads != 1: the same taps added on all cores (threads=0) or that many
+    (3D positions only)."""
     grid = np.zeros((dims, dims, dims), np.float64)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    if threads != 1 and pos.shape[1] == 3:
+        lib = _load()
+        Wc = None if W is None else np.ascontiguousarray(W, dtype=np.float32)
+        lib.orc_deposit_d_omp({"NGP": 1, "CIC": 2, "TSC": 3, "PCS": 4}[MAS], pos.ctypes.data,
+                              pos.shape[0], _ptr(Wc), grid.ctypes.data, dims,
+                              float(np.float32(BoxSize)), int(threads))
+        return grid
     _deposit(MAS, pos, grid, BoxSize, W, f64=True)
     return grid
 

@@ -13,6 +13,8 @@
  *        TSC :369-404, TSCW :417-452, PCS :463-497, PCSW :510-545
  *   orc_*_d (float64 grid)                 <- NGPW_d :338-358, CICW_d :229-266
  *        (extended here to TSC/PCS for the float64 precision oracle)
+ *   orc_deposit_d_omp                      the orc_*_d taps on all cores (3D),
+ *        float64 atomics; for the precision oracle on large grids
  *   orc_deposit_omp                        <- library/MAS_library/MAS_c.c:8-266
  *        (OpenMP particle loop with an atomic add per tap)
  *   orc_pk_bin                             <- library/Pk_library/Pk_library.pyx:311-378
@@ -201,6 +203,58 @@ void orc_pcs_d(const float *pos, long n, int coord, const float *W, double *g,
 {
     int dz = (coord == 3) ? dims : 1;
     DEPOSIT_BODY_SPLINE(4, pcs_axis)
+}
+
+/* ------------------------------------------------------------------------ */
+/* Float64 grid deposit on all cores, 3D only (precision oracle for large
+ * grids): the per-tap values of orc_ngp_d .. orc_pcs_d above, each added with
+ * `#pragma omp atomic`; the result differs from the serial functions only by
+ * the float64 rounding order.  mas: 1 NGP 2 CIC 3 TSC 4 PCS                */
+/* ------------------------------------------------------------------------ */
+void orc_deposit_d_omp(int mas, const float *pos, long n, const float *W,
+                       double *g, int dims, float box, int threads)
+{
+    const float inv_cell_size = dims / box;
+    const long sx = (long)dims * dims, sy = dims;
+#ifdef _OPENMP
+    if (threads < 1) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(static, 4096)
+#endif
+    for (long i = 0; i < n; i++) {
+        const float w = W ? W[i] : 1.0f;
+        float C[3][4];
+        int index[3][4];
+        int nt = 4;
+        for (int ax = 0; ax < 3; ax++) {
+            const float dist = pos[3*i+ax] * inv_cell_size;
+            if (mas == 1) {
+                nt = 1;
+                index[ax][0] = ((int)((double)dist + 0.5) + dims) % dims;
+                C[ax][0] = 1.0f;
+            } else if (mas == 2) {
+                nt = 2;
+                C[ax][1] = dist - (float)(int)dist;
+                C[ax][0] = (float)(1.0 - (double)C[ax][1]);
+                index[ax][0] = ((int)dist) % dims;
+                index[ax][1] = (index[ax][0] + 1) % dims;
+            } else if (mas == 3) {
+                nt = 3;
+                tsc_axis(dist, dims, index[ax], C[ax]);
+            } else {
+                pcs_axis(dist, dims, index[ax], C[ax]);
+            }
+        }
+        for (int l = 0; l < nt; l++)
+            for (int m = 0; m < nt; m++)
+                for (int q = 0; q < nt; q++) {
+                    float v = C[0][l]*C[1][m]*C[2][q];
+                    if (W) v = v * w;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                    g[index[0][l]*sx + index[1][m]*sy + index[2][q]] += v;
+                }
+    }
 }
 
 /* ------------------------------------------------------------------------ */

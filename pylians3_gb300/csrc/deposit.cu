@@ -34,11 +34,13 @@ namespace {
 constexpr int kThreads = 256;
 
 // ------------------------------------------------------------ unsorted path
-template <int MAS, bool HAS_W, typename G>
+// COMP: compensated float adds, errors into lo (same layout as the grid).
+template <int MAS, bool HAS_W, typename G, bool COMP>
 __global__ void __launch_bounds__(kThreads)
 k_deposit_atomic(const float *__restrict__ pos, long long n, int coord,
                  const float *__restrict__ W, G *__restrict__ grid, int dims,
-                 float inv) {
+                 float inv, float *__restrict__ lo) {
+    static_assert(!COMP || sizeof(G) == sizeof(float), "compensation is for float32 grids");
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
     const long long sy = coord == 3 ? dims : 1;
@@ -81,16 +83,26 @@ k_deposit_atomic(const float *__restrict__ pos, long long n, int coord,
 #pragma unroll
             for (int m = 0; m < NT; ++m) {
                 const float wxy = wx[l] * wy[m];
-                G *row = grid + ix[l] * sx + iy[m] * sy;
+                const long long row = ix[l] * sx + iy[m] * sy;
 #pragma unroll
                 for (int q = 0; q < NT; ++q) {
                     float v = wxy * wz[q];
                     if (HAS_W) v *= wt;
-                    atomicAdd(row + iz[q], (G)v);
+                    if constexpr (COMP)
+                        comp_add(reinterpret_cast<float *>(grid) + row + iz[q], lo + row + iz[q], v);
+                    else
+                        atomicAdd(grid + row + iz[q], (G)v);
                 }
             }
         }
     }
+}
+
+// g += lo elementwise (one rounding): folds the compensation into the grid
+__global__ void k_fold_lo(float *__restrict__ g, const float *__restrict__ lo, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x)
+        g[i] = __fadd_rn(g[i], lo[i]);
 }
 
 // g /= d elementwise (IEEE division, as numpy's `number2 /= 2.0` on float32)
@@ -112,19 +124,29 @@ int scale_t(pyl_ctx *ctx, G *grid, int64_t count, G s) {
     return PYL_OK;
 }
 
+// lo != nullptr (float grids only): compensated adds, errors into lo.
 template <int MAS, typename G>
 int launch_atomic(pyl_ctx *ctx, const float *pos, long long n, int coord, const float *W,
-                  G *grid, int dims, float inv) {
+                  G *grid, int dims, float inv, float *lo) {
     long long blocks = (n + kThreads - 1) / kThreads;
     if (blocks > 152LL * 64) blocks = 152LL * 64;
     if (blocks < 1) blocks = 1;
     StageScope s(ctx, ST_DEPOSIT);
-    if (W)
-        k_deposit_atomic<MAS, true, G><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(
-            pos, n, coord, W, grid, dims, inv);
-    else
-        k_deposit_atomic<MAS, false, G><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(
-            pos, n, coord, W, grid, dims, inv);
+    auto go = [&](auto kernel) {
+        kernel<<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(pos, n, coord, W, grid, dims, inv,
+                                                               lo);
+    };
+    if constexpr (sizeof(G) == sizeof(float)) {
+        if (lo) {
+            if (W) go(k_deposit_atomic<MAS, true, G, true>);
+            else go(k_deposit_atomic<MAS, false, G, true>);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+            return PYL_OK;
+        }
+    }
+    if (W) go(k_deposit_atomic<MAS, true, G, false>);
+    else go(k_deposit_atomic<MAS, false, G, false>);
     ctx->launches++;
     PYL_CUDA(ctx, cudaGetLastError());
     return PYL_OK;
@@ -601,12 +623,20 @@ __device__ __forceinline__ int box_line(int *a, int n, int st, bool write) {
 // sums are exact (independent of the order of the atomics); the flush
 // converts each cell once (int -> float rounding, then an exact scaling by
 // 2^-e).
-template <int MAS, bool HAS_W, bool FIXED>
+//
+// COMP (PYL_COMPENSATED): float shared accumulators with a second footprint
+// of TwoSum rounding errors (comp_add), merged into the grid and into the
+// error grid glo with compensated global atomics.
+constexpr int kAccFloat = 0, kAccFixed = 1, kAccComp = 2;
+
+template <int MAS, bool HAS_W, int ACC>
 __global__ void __launch_bounds__(512)
 k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                const unsigned *__restrict__ start, const uint2 *__restrict__ items,
                const unsigned *__restrict__ nitems, float inv, TileGeom g,
-               float *__restrict__ grid, int vec4) {
+               float *__restrict__ grid, int vec4, float *__restrict__ glo) {
+    constexpr bool FIXED = ACC == kAccFixed;
+    constexpr bool COMP = ACC == kAccComp;
     static_assert(!(FIXED && HAS_W), "fixed-point accumulation is for unit weights");
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
@@ -619,7 +649,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
     for (unsigned it = blockIdx.x; it < total; it += gridDim.x) {
         const uint2 item = items[it];
         const int t = (int)item.x;
-        for (int i = threadIdx.x; i < cells; i += blockDim.x) s_reg[i] = 0.f;
+        for (int i = threadIdx.x; i < (COMP ? 2 : 1) * cells; i += blockDim.x) s_reg[i] = 0.f;
         const int tx = t / (g.nty * g.ntz), ty = (t / g.ntz) % g.nty, tz = t % g.ntz;
         const int ox = tx * g.TX, oy = ty * g.TY, oz = tz * g.TZ;   // tile origin (cells)
         const long long p0 = (long long)start[t] + (long long)item.y * kItemCap;
@@ -719,6 +749,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                         float v = wxy * wz[q];
                         if (HAS_W) v *= wt;
                         if (FIXED) atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
+                        else if (COMP) comp_add(s_reg + row + lz[q], s_reg + cells + row + lz[q], v);
                         else atomicAdd(s_reg + row + lz[q], v);
                     }
                 }
@@ -748,7 +779,19 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         const int d = g.dims;
         const long long dd = (long long)d * d;
         const int zs = oz - S::LO;  // unwrapped global z of footprint column 0
-        if (vec4) {
+        if (COMP) {
+            for (int c = threadIdx.x; c < cells; c += blockDim.x) {
+                const float v = s_reg[c], e = s_reg[cells + c];
+                if (v == 0.f && e == 0.f) continue;
+                const int lz = c % RZ, ly = (c / RZ) % RY, lx = c / (RZ * RY);
+                const int gx = wrap_idx(ox - S::LO + lx, d);
+                const int gy = wrap_idx(oy - S::LO + ly, d);
+                const int gz = wrap_idx(zs + lz, d);
+                const long long gi = gx * dd + (long long)gy * d + gz;
+                comp_add(grid + gi, glo + gi, v);
+                if (e != 0.f) atomicAdd(glo + gi, e);
+            }
+        } else if (vec4) {
             // quads aligned to the global z index (dims % 4 == 0: never wraps inside)
             const int q0 = (zs >= 0 ? zs : zs - 3) / 4;          // floor(zs / 4)
             const int q1 = (zs + RZ - 1 >= 0 ? zs + RZ - 1 : zs + RZ - 4) / 4;
@@ -842,7 +885,8 @@ size_t partition_smem(bool weighted) {
 
 template <int MAS, bool HAS_W>
 int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
-                    int dims, float inv, const TileGeom &g, int forced_mode, bool fixed) {
+                    int dims, float inv, const TileGeom &g, int forced_mode, int acc,
+                    float *glo) {
     int st = PYL_OK;
     const int nt = g.ntiles;
     const bool two_pass = forced_mode != kSortFrontier;   // may be chosen on the device
@@ -939,7 +983,8 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         }
     }
     const int vec4 = (dims % 4 == 0 && ((uintptr_t)grid & 15) == 0) ? 1 : 0;
-    const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
+    const size_t rsm =
+        sizeof(float) * (size_t)g.RX * g.RY * g.RZ * (acc == kAccComp ? 2 : 1);
     auto run = [&](auto kernel) -> int {
         int st2;
         if ((st2 = set_smem(ctx, kernel, rsm))) return st2;
@@ -949,34 +994,42 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         if (grid_n > (long long)max_items) grid_n = (long long)max_items;
         StageScope s(ctx, ST_DEPOSIT);
         kernel<<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(b2, w2, start, items, nitems, inv, g,
-                                                           grid, vec4);
+                                                           grid, vec4, glo);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         return PYL_OK;
     };
+    if (acc == kAccComp) return run(k_tile_deposit<MAS, HAS_W, kAccComp>);
     if constexpr (!HAS_W) {
-        if (fixed) return run(k_tile_deposit<MAS, false, true>);
+        if (acc == kAccFixed) return run(k_tile_deposit<MAS, false, kAccFixed>);
     }
-    return run(k_tile_deposit<MAS, HAS_W, false>);
+    return run(k_tile_deposit<MAS, HAS_W, kAccFloat>);
 }
 
 template <int MAS>
 int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
-                  int dims, float inv, int flags) {
+                  int dims, float inv, int flags, float *glo) {
     const TileGeom g = make_geom(dims, MAS);
     const int forced = (flags & PYL_SORT_TWO_PASS) ? kSortTwoPass
                        : (flags & PYL_SORT_FRONTIER) ? kSortFrontier : -1;
-    // unit weights accumulate in fixed point unless float atomics are asked for
-    const bool fixed = !(flags & PYL_DEPOSIT_FLOAT);
-    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced, false)
-             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced, fixed);
+    // Compensated if asked for; else unit weights accumulate in fixed point
+    // (NGP/CIC/TSC) unless float atomics are asked for.  PCS keeps float
+    // atomics: its deconvolution amplifies the grid's rounding noise ~5e4-fold
+    // in the corner bins beyond the Nyquist wavenumber, and the coarser
+    // quantization of tiles holding dense halos shows there.
+    const int acc = glo ? kAccComp
+                        : (!W && MAS != PYL_MAS_PCS && !(flags & PYL_DEPOSIT_FLOAT)) ? kAccFixed
+                                                                                    : kAccFloat;
+    return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo)
+             : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo);
 }
 
 bool use_sorted(long long n, int coord, int dims, int mas, int flags) {
     if (coord != 3) return false;
     if (flags & PYL_DEPOSIT_ATOMIC) return false;
     const TileGeom g = make_geom(dims, mas);
-    const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
+    const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ *
+                       ((flags & PYL_COMPENSATED) ? 2 : 1);
     if (rsm > 200 * 1024 || (size_t)g.ntiles * 4 > 200 * 1024) return false;
     if (g.F > 65535 || g.ncoarse > kMaxKeys) return false;
     if (n >= (1LL << 32) - 1) return false;
@@ -989,26 +1042,44 @@ bool use_sorted(long long n, int coord, int dims, int mas, int flags) {
 template <typename G>
 static int deposit_t(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
                      G *grid, int dims, float BoxSize, int mas, int flags) {
+    if (mas < PYL_MAS_NGP || mas > PYL_MAS_PCS)
+        return fail(ctx, PYL_ERR_ARG, "option not valid!!! (MAS must be NGP, CIC, TSC or PCS)");
     if (n == 0) return PYL_OK;
     // inv_cell_size = dims/BoxSize as a float division (MAS_library.pyx:135)
     const float inv = (float)dims / BoxSize;
+    int st = PYL_OK;
+    // compensated float32 deposit: rounding errors into lo, folded at the end
+    float *lo = nullptr;
+    const long long cells = (long long)dims * dims * (coord == 3 ? dims : 1);
+    if (sizeof(G) == sizeof(float) && (flags & PYL_COMPENSATED)) {
+        lo = (float *)ws_get(ctx, "dep_lo", sizeof(float) * (size_t)cells, &st);
+        if (!lo) return st;
+        PYL_CUDA(ctx, cudaMemsetAsync(lo, 0, sizeof(float) * (size_t)cells, ctx->stream));
+    }
     if (sizeof(G) == sizeof(float) && use_sorted(n, coord, dims, mas, flags)) {
         float *gf = reinterpret_cast<float *>(grid);
         switch (mas) {
-            case PYL_MAS_NGP: return launch_sorted<PYL_MAS_NGP>(ctx, pos, n, W, gf, dims, inv, flags);
-            case PYL_MAS_CIC: return launch_sorted<PYL_MAS_CIC>(ctx, pos, n, W, gf, dims, inv, flags);
-            case PYL_MAS_TSC: return launch_sorted<PYL_MAS_TSC>(ctx, pos, n, W, gf, dims, inv, flags);
-            case PYL_MAS_PCS: return launch_sorted<PYL_MAS_PCS>(ctx, pos, n, W, gf, dims, inv, flags);
-            default: break;
+            case PYL_MAS_NGP: st = launch_sorted<PYL_MAS_NGP>(ctx, pos, n, W, gf, dims, inv, flags, lo); break;
+            case PYL_MAS_CIC: st = launch_sorted<PYL_MAS_CIC>(ctx, pos, n, W, gf, dims, inv, flags, lo); break;
+            case PYL_MAS_TSC: st = launch_sorted<PYL_MAS_TSC>(ctx, pos, n, W, gf, dims, inv, flags, lo); break;
+            default: st = launch_sorted<PYL_MAS_PCS>(ctx, pos, n, W, gf, dims, inv, flags, lo); break;
+        }
+    } else {
+        switch (mas) {
+            case PYL_MAS_NGP: st = launch_atomic<PYL_MAS_NGP>(ctx, pos, n, coord, W, grid, dims, inv, lo); break;
+            case PYL_MAS_CIC: st = launch_atomic<PYL_MAS_CIC>(ctx, pos, n, coord, W, grid, dims, inv, lo); break;
+            case PYL_MAS_TSC: st = launch_atomic<PYL_MAS_TSC>(ctx, pos, n, coord, W, grid, dims, inv, lo); break;
+            default: st = launch_atomic<PYL_MAS_PCS>(ctx, pos, n, coord, W, grid, dims, inv, lo); break;
         }
     }
-    switch (mas) {
-        case PYL_MAS_NGP: return launch_atomic<PYL_MAS_NGP>(ctx, pos, n, coord, W, grid, dims, inv);
-        case PYL_MAS_CIC: return launch_atomic<PYL_MAS_CIC>(ctx, pos, n, coord, W, grid, dims, inv);
-        case PYL_MAS_TSC: return launch_atomic<PYL_MAS_TSC>(ctx, pos, n, coord, W, grid, dims, inv);
-        case PYL_MAS_PCS: return launch_atomic<PYL_MAS_PCS>(ctx, pos, n, coord, W, grid, dims, inv);
-        default: return fail(ctx, PYL_ERR_ARG, "option not valid!!! (MAS must be NGP, CIC, TSC or PCS)");
-    }
+    if (st || !lo) return st;
+    long long blocks = (cells + kThreads - 1) / kThreads;
+    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    k_fold_lo<<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(reinterpret_cast<float *>(grid), lo,
+                                                             cells);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
 }
 
 int deposit(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,

@@ -13,9 +13,10 @@
 //   PCS: minimum = floor(dist - 2) = c - 2, taps minimum+1 .. minimum+4,
 //        w = (4 - 6 diff^2 + 3 diff^3)/6 | (2 - diff)^3 / 6 | 0  (:484-492)
 // The cell choice is exact (the reference decides it with the same float
-// product and exact integer comparisons); the spline polynomials are
-// evaluated in float32 (the reference: double, rounded to float), i.e. at
-// most one ulp per weight.
+// product and exact integer comparisons).  The NGP, CIC and TSC weights are
+// the reference's float values exactly (their double steps are exact or
+// rounded once); the PCS cubics are evaluated in float32 (the reference: in
+// double, rounded to float), within a couple of ulps per weight.
 #pragma once
 
 #include "common.cuh"
@@ -72,7 +73,9 @@ __device__ __forceinline__ void axis_stencil(float dist, int c, int *off, float 
             const int t = minimum + j + 1;
             const float diff = fabsf((float)t - dist);
             float C;
-            if (diff < 0.5f) C = 0.75f - diff * diff;
+            // 0.75 - diff*diff with the product rounded first, as the reference
+            // (float product, double subtraction exact here, one rounding)
+            if (diff < 0.5f) C = __fsub_rn(0.75f, __fmul_rn(diff, diff));
             else if (diff < 1.5f) { const float q = 1.5f - diff; C = 0.5f * q * q; }
             else C = 0.f;
             off[j] = t - c;
@@ -92,6 +95,19 @@ __device__ __forceinline__ void axis_stencil(float dist, int c, int *off, float 
             w[j] = C;
         }
     }
+}
+
+// Compensated accumulation (PYL_COMPENSATED): adds v to *hi with an atomic,
+// recomputes the rounded sum the atomic formed from the value it read, and
+// adds the rounding error of that addition (Knuth's TwoSum) to *lo.  hi + lo
+// then holds the exact sum of everything added, up to the rounding of the
+// much smaller lo sums.  Works on shared and global addresses.
+__device__ __forceinline__ void comp_add(float *hi, float *lo, float v) {
+    const float old = atomicAdd(hi, v);
+    const float s = __fadd_rn(old, v);
+    const float bv = __fsub_rn(s, old);
+    const float err = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bv)), __fsub_rn(v, bv));
+    if (err != 0.f) atomicAdd(lo, err);
 }
 
 }  // namespace pyl

@@ -106,3 +106,27 @@ def test_sorted_unaligned_device_grid(native, oracle):
     assert float(buf[0].item()) == 0.0
     got = view.cpu().numpy().reshape((dims,) * 3)
     assert float(np.abs(got - ref).max()) <= 1e-5 * float(ref.max())
+
+
+@pytest.mark.parametrize("MAS", ["NGP", "CIC", "TSC", "PCS"])
+@pytest.mark.parametrize("path", ["sorted", "atomic"])
+def test_compensated_matches_float64(native, oracle, MAS, path):
+    """PYL_COMPENSATED: every cell is the float64 sum of its taps rounded
+    once to float32, also in cells holding thousands of particles (where the
+    plain float32 sums drift by many ulps).  NGP/CIC/TSC taps equal the
+    reference's; PCS taps carry the float32 evaluation of the cubic (a few
+    ulps each), which the bound adds for PCS."""
+    rng = np.random.default_rng(17)
+    c = rng.random((8, 3)) * BOX
+    pos = np.concatenate([
+        np.mod(c[rng.integers(0, 8, 400000)] + rng.standard_normal((400000, 3)) * 3.0, BOX),
+        rng.random((200000, 3)) * BOX]).astype(np.float32)
+    W = rng.lognormal(0, 0.5, len(pos)).astype(np.float32)
+    flag = native.PYL_DEPOSIT_SORTED if path == "sorted" else native.PYL_DEPOSIT_ATOMIC
+    for w in (None, W):
+        ref64 = oracle.MA_f64(pos, 64, BOX, MAS, W=w)
+        g = run_ma(native, pos, 64, MAS, w, flag | native.PYL_COMPENSATED)
+        ulp = np.spacing(np.abs(ref64).astype(np.float32)).astype(np.float64)
+        tol = 1.0 * ulp + (8 * 2.0 ** -24 * np.abs(ref64) if MAS == "PCS" else 0.0)
+        err = np.abs(g.astype(np.float64) - ref64)
+        assert np.all(err <= tol), (MAS, path, w is None, float((err / ulp).max()))

@@ -111,3 +111,15 @@ def test_omp_deposit_matches_serial(oracle):
         oracle.MA(pos, a, BOX, MAS)
         oracle.deposit_omp(MAS, pos, b, BOX, threads=2)
         assert np.abs(a - b).max() < 1e-5
+
+
+def test_f64_omp_deposit_matches_serial(oracle):
+    """The all-cores float64 deposit adds the same taps as the serial one."""
+    rng = np.random.default_rng(10)
+    pos = rng.random((20000, 3), dtype=np.float32) * np.float32(BOX)
+    W = rng.lognormal(0, 0.5, len(pos)).astype(np.float32)
+    for MAS in ("NGP", "CIC", "TSC", "PCS"):
+        for w in (None, W):
+            a = oracle.MA_f64(pos, 20, BOX, MAS, W=w)
+            b = oracle.MA_f64(pos, 20, BOX, MAS, W=w, threads=2)
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
