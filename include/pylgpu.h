@@ -208,6 +208,52 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms);
 int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double BoxSize,
                    int axis, int mas, int what, pyl_pk_out *out);
 
+/* ---------------------------------------------------------------------
+ * Rows around the spectrum (same FFT, window and mode conventions).
+ * ------------------------------------------------------------------- */
+
+/* correct_MAS (library/Pk_library/Pk_library.pyx:1882-1939): out = the
+ * field with its independent Fourier modes divided by the MAS window
+ * (r2c, window, c2r normalised by 1/dims^3).  delta is not modified.      */
+int pyl_correct_mas(pyl_ctx *ctx, const float *delta, float *out, int dims,
+                    int mas, int flags);
+
+/* FFT2Dr_f / IFFT2Dr_f (Pk_library.pyx:181-196, 213-228): (grid, grid)
+ * float32 <-> (grid, grid/2+1) complex64 (interleaved floats); the inverse
+ * is normalised by 1/grid^2 and does not modify its input.                */
+int pyl_fft2_r2c(pyl_ctx *ctx, const float *in, float *out, int grid, int flags);
+int pyl_fft2_c2r(pyl_ctx *ctx, const float *in, float *out, int grid, int flags);
+
+/* class Pk_plane (Pk_library.pyx:435-511): spectrum of a (grid, grid)
+ * float32 field; k, Pk, Nmodes have kmax = int(sqrt(2 (grid/2)^2)) entries
+ * (the DC bin dropped).  Returns PYL_ERR_MODES when check_number_modes_2D
+ * (:102-115) would exit.                                                   */
+int pyl_pk_plane(pyl_ctx *ctx, const float *delta, int grid, double BoxSize,
+                 int mas, double *k, double *Pk, double *Nmodes, int flags);
+
+/* CIC_interp (library/MAS_library/MAS_library.pyx:558-599): den[i] = the
+ * trilinear (CIC) interpolation of density (dims^3 float32) at pos[i]
+ * ((n, 3) float32), float32 arithmetic in the reference's order.          */
+int pyl_cic_interp(pyl_ctx *ctx, const float *density, int dims, float BoxSize,
+                   const float *pos, int64_t n, float *den, int flags);
+
+/* class XPk (Pk_library.pyx:529-735): auto- and cross-spectra of nfields
+ * (1..8) float32 fields of the same dims^3 grid, mas[i] the window of field
+ * i.  With X = nfields (nfields - 1) / 2 pairs (i < j in row order), the
+ * row-major arrays are: Pk (kmax, 3, nfields), XPk (kmax, 3, X), k3D and
+ * Nmodes3D (kmax); k1D, Nmodes1D (kmax_par), Pk1D (kmax_par, nfields), PkX1D
+ * (kmax_par, X); kpar, kper, Nmodes2D (n2D), Pk2D (n2D, nfields), PkX2D
+ * (n2D, X), n2D = (kmax_par + 1)(kmax_per + 1).  Null pointers skip an
+ * output.  deltas[i] are host pointers, or device pointers with
+ * PYL_DEVICE_PTRS.                                                         */
+typedef struct {
+    double *k3D, *Pk, *XPk, *Nmodes3D;
+    double *k1D, *Pk1D, *PkX1D, *Nmodes1D;
+    double *kpar, *kper, *Pk2D, *PkX2D, *Nmodes2D;
+} pyl_xpk_out;
+int pyl_xpk(pyl_ctx *ctx, const float *const *deltas, int nfields, int dims,
+            double BoxSize, int axis, const int *mas, pyl_xpk_out *out, int flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -282,3 +282,193 @@ class Pk_f64:
         self.Pk = np.stack([Pk3D[:, 0] / N3D * unit, Pk3D[:, 1] * 5.0 / N3D * unit,
                             Pk3D[:, 2] * 9.0 / N3D * unit], axis=1)
         self.Nmodes3D = N3D
+
+
+# --------------------------------------------------------------------------
+# Rows around the spectrum (numpy restatements; small grids)
+# --------------------------------------------------------------------------
+def _window_1d(dims, MAS_index, nonneg=False):
+    """MAS_correction(pi k / dims, p) in double for every index (Pk_library.pyx:83-84)."""
+    middle = dims // 2
+    idx = np.arange(dims // 2 + 1 if nonneg else dims)
+    k = idx if nonneg else np.where(idx > middle, idx - dims, idx)
+    x = (np.pi / dims) * k
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = np.where(x == 0.0, 1.0, np.power(x / np.sin(np.where(x == 0, 1.0, x)), MAS_index))
+    return k, w
+
+
+def _independent(kx, ky, kz, dims):
+    """Hermitian half-space selection of the mode loops (Pk_library.pyx:324-327)."""
+    middle, even = dims // 2, dims % 2 == 0
+    plane = (kz == 0) | ((kz == middle) & even)
+    edge = (kx == 0) | ((kx == middle) & even)
+    return ~(plane & ((kx < 0) | (edge & (ky < 0))))
+
+
+def correct_MAS(delta, BoxSize, MAS="CIC", threads=1):
+    """Restatement of correct_MAS (Pk_library.pyx:1882-1939)."""
+    dims = delta.shape[0]
+    p = MAS_function(MAS)
+    dk = FFT3Dr_f(delta, threads)
+    kx, wx = _window_1d(dims, p)
+    kz, wz = _window_1d(dims, p, nonneg=True)
+    KX, KY, KZ = np.meshgrid(kx, kx, kz, indexing="ij")
+    fac = ((wx[:, None, None] * wx[None, :, None]) * wz[None, None, :]).astype(np.float32)
+    m = _independent(KX, KY, KZ, dims)
+    dk[m] = dk[m] * fac[m]
+    return IFFT3Dr_f(dk, threads)
+
+
+def FFT2Dr_f(a, threads=1):
+    """r2c over (0,1), unnormalised, complex64 (Pk_library.pyx:181-196)."""
+    import scipy.fft as sf
+    return sf.rfftn(np.asarray(a, np.float32), axes=(0, 1),
+                    workers=max(1, int(threads))).astype(np.complex64, copy=False)
+
+
+def IFFT2Dr_f(a, threads=1):
+    """c2r normalised by 1/N^2, float32 (Pk_library.pyx:213-228)."""
+    import scipy.fft as sf
+    g = a.shape[0]
+    return sf.irfftn(np.asarray(a, np.complex64), s=(g, g), axes=(0, 1),
+                     workers=max(1, int(threads))).astype(np.float32, copy=False)
+
+
+class Pk_plane:
+    """Restatement of class Pk_plane (Pk_library.pyx:435-511): k, Pk, Nmodes."""
+
+    def __init__(self, delta, BoxSize, MAS="CIC", threads=1, verbose=False):
+        grid = delta.shape[0]
+        middle, even = grid // 2, grid % 2 == 0
+        kF = 2.0 * np.pi / BoxSize
+        kmax = int(np.sqrt(middle ** 2 + middle ** 2))
+        p = MAS_function(MAS)
+        dk = FFT2Dr_f(delta, threads)
+        kx, wx = _window_1d(grid, p)
+        ky, wy = _window_1d(grid, p, nonneg=True)
+        KX, KY = np.meshgrid(kx, ky, indexing="ij")
+        keep = ~(((KY == 0) | ((KY == middle) & even)) & (KX < 0))
+        k = np.sqrt((KX * KX + KY * KY).astype(np.float64))
+        kidx = k.astype(np.int64)
+        fac = (wx[:, None] * wy[None, :]).astype(np.float32)
+        v = (dk * fac)[keep]
+        d2 = v.real.astype(np.float64) ** 2 + v.imag.astype(np.float64) ** 2
+        ki = kidx[keep]
+        N = np.bincount(ki, minlength=kmax + 1).astype(np.float64)
+        ks = np.bincount(ki, weights=k[keep], minlength=kmax + 1)
+        P = np.bincount(ki, weights=d2, minlength=kmax + 1)
+        if int(N.sum()) != (grid * grid - (1 if grid % 2 else 4)) // 2 + (1 if grid % 2 else 4):
+            raise RuntimeError("not all modes counted")
+        N, ks, P = N[1:], ks[1:], P[1:]
+        self.k = ks / N * kF
+        self.Pk = P / N * (BoxSize / grid ** 2) ** 2
+        self.Nmodes = N
+
+
+class XPk:
+    """Restatement of class XPk (Pk_library.pyx:529-735), vectorised over the
+    modes (float64 sums in another order than the reference's loop)."""
+
+    def __init__(self, delta, BoxSize, axis=2, MAS=None, threads=1):
+        fields = len(delta)
+        dims = delta[0].shape[0]
+        middle = dims // 2
+        kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
+        kx, _ = _window_1d(dims, 0)
+        kz, _ = _window_1d(dims, 0, nonneg=True)
+        KX, KY, KZ = np.meshgrid(kx, kx, kz, indexing="ij")
+        keep = _independent(KX, KY, KZ, dims)
+        KX, KY, KZ = KX[keep], KY[keep], KZ[keep]
+        k = np.sqrt((KX * KX + KY * KY + KZ * KZ).astype(np.float64))
+        kidx = k.astype(np.int64)
+        kpar = {0: KX, 1: KY}.get(axis, KZ)
+        kper2 = {0: KY * KY + KZ * KZ, 1: KX * KX + KZ * KZ}.get(axis, KX * KX + KY * KY)
+        kper = np.sqrt(kper2.astype(np.float64)).astype(np.int64)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            mu = np.where(k == 0, 0.0, kpar / np.where(k == 0, 1.0, k))
+        mu2 = mu * mu
+        val1 = (3.0 * mu2 - 1.0) / 2.0
+        val2 = (35.0 * mu2 * mu2 - 30.0 * mu2 + 3.0) / 8.0
+        apar = np.abs(kpar)
+        in1 = k <= middle
+        i2 = (kmax_par + 1) * kper + apar
+        re, im = [], []
+        for f, m in zip(delta, MAS):
+            p = MAS_function(m)
+            _, wx = _window_1d(dims, p)
+            _, wz = _window_1d(dims, p, nonneg=True)
+            fac = ((wx[:, None, None] * wx[None, :, None]) * wz[None, None, :]).astype(np.float32)
+            v = (FFT3Dr_f(f, threads) * fac)[keep]
+            re.append(v.real.astype(np.float64))
+            im.append(v.imag.astype(np.float64))
+        series = [re[i] * re[i] + im[i] * im[i] for i in range(fields)]
+        for i in range(fields):
+            for j in range(i + 1, fields):
+                series.append(re[i] * re[j] + im[i] * im[j])
+        n2d = (kmax_par + 1) * (kmax_per + 1)
+
+        def binned(idx, w, n):
+            return np.bincount(idx, weights=w, minlength=n)
+
+        N3 = binned(kidx, None, kmax + 1).astype(np.float64)
+        k3 = binned(kidx, k, kmax + 1)
+        N1 = binned(apar[in1], None, kmax_par + 1).astype(np.float64)
+        k1 = binned(apar[in1], apar[in1].astype(np.float64), kmax_par + 1)
+        N2 = binned(i2, None, n2d).astype(np.float64)
+        S = len(series)
+        P3 = np.zeros((kmax + 1, 3, S))
+        P1 = np.zeros((kmax_par + 1, S))
+        P2 = np.zeros((n2d, S))
+        for s, d2 in enumerate(series):
+            P3[:, 0, s] = binned(kidx, d2, kmax + 1)
+            P3[:, 1, s] = binned(kidx, d2 * val1, kmax + 1)
+            P3[:, 2, s] = binned(kidx, d2 * val2, kmax + 1)
+            P1[:, s] = binned(apar[in1], d2[in1], kmax_par + 1)
+            P2[:, s] = binned(i2, d2, n2d)
+        if int(N3.sum()) != expected_modes(dims):
+            raise RuntimeError("not all modes counted")
+        fact = (BoxSize / dims ** 2) ** 3
+        k1D = k1[1:] / N1[1:] * kF
+        kmaxper = np.sqrt(kN ** 2 - k1D ** 2)
+        P1 = P1[1:] * fact
+        P1 = P1 * (np.pi * kmaxper[:, None] ** 2 / N1[1:, None]) / (2.0 * np.pi) ** 2
+        self.k1D, self.Nmodes1D = k1D, N1[1:]
+        self.Pk1D, self.PkX1D = P1[:, :fields], P1[:, fields:]
+        pp = np.arange(kmax_par + 1)
+        qq = np.arange(kmax_per + 1)
+        idx2 = (kmax_par + 1) * qq[None, :] + pp[:, None]
+        self.kpar = np.zeros(n2d)
+        self.kper = np.zeros(n2d)
+        self.kpar[idx2] = (0.5 * (pp + pp + 1) * kF)[:, None]
+        self.kper[idx2] = (0.5 * (qq + qq + 1) * kF)[None, :]
+        P2 = P2 * fact / N2[:, None]
+        self.Pk2D, self.PkX2D, self.Nmodes2D = P2[:, :fields], P2[:, fields:], N2
+        N3, k3, P3 = N3[1:], k3[1:], P3[1:]
+        self.k3D = k3 / N3 * kF
+        scale = np.array([1.0, 5.0, 9.0])[None, :, None]
+        P3 = (P3 * scale / N3[:, None, None]) * fact
+        self.Pk, self.XPk, self.Nmodes3D = P3[:, :, :fields], P3[:, :, fields:], N3
+
+
+def CIC_interp(density, BoxSize, pos, den):
+    """Restatement of CIC_interp (MAS_library.pyx:558-599), float32 steps in
+    the written order; writes den in place."""
+    dims = density.shape[0]
+    inv = np.float32(np.float32(dims) / np.float32(BoxSize))
+    pos = np.asarray(pos, np.float32)
+    dist = pos * inv
+    c = dist.astype(np.int32)
+    u = (dist - c.astype(np.float32)).astype(np.float32)
+    d = (np.float32(1.0) - u).astype(np.float32)
+    lo = c % dims
+    hi = (lo + 1) % dims
+    g = density
+    terms = [
+        (lo, lo, lo, d, d, d), (lo, lo, hi, d, d, u), (lo, hi, lo, d, u, d), (lo, hi, hi, d, u, u),
+        (hi, lo, lo, u, d, d), (hi, lo, hi, u, d, u), (hi, hi, lo, u, u, d), (hi, hi, hi, u, u, u)]
+    s = None
+    for ix, iy, iz, a, b, cc in terms:
+        t = g[ix[:, 0], iy[:, 1], iz[:, 2]] * a[:, 0] * b[:, 1] * cc[:, 2]
+        s = t if s is None else (s + t).astype(np.float32)
+    den[:len(s)] = s

@@ -9,6 +9,8 @@ library/MAS_library/MAS_library.pyx:
   * ``NGPW_d/CICW_d`` with a float64 grid (:229-266, :338-358).
   * ``NGPc3D..PCSWc3D(pos, number, BoxSize, threads)`` (:1305-1389): the
     reference's OpenMP entry points; ``threads`` is accepted and ignored.
+  * ``CIC_interp(density, BoxSize, pos, den)`` (:558-599): trilinear
+    interpolation of a grid at the positions, written into ``den``.
 The deposit runs on the GPU (libpylgpu.so, pyl_ma); there is no CPU path.
 ``pos``/``number``/``W`` may be numpy arrays or torch CUDA tensors.
 """
@@ -26,7 +28,7 @@ from ._arrays import (dev_ptr, host_ptr, is_cuda_tensor, is_tensor, require_dtyp
 
 __all__ = ["MA", "NGP", "CIC", "TSC", "PCS", "NGPW", "CICW", "TSCW", "PCSW",
            "NGPW_d", "CICW_d", "NGPc3D", "CICc3D", "TSCc3D", "PCSc3D",
-           "NGPWc3D", "CICWc3D", "TSCWc3D", "PCSWc3D", "FLOAT_type"]
+           "NGPWc3D", "CICWc3D", "TSCWc3D", "PCSWc3D", "FLOAT_type", "CIC_interp"]
 
 _RENORM = {"NGP": 1.0, "CIC": 2.0, "TSC": 3.0, "PCS": 4.0}
 
@@ -207,3 +209,40 @@ def PCSc3D(pos, number, BoxSize, threads=1):
 def PCSWc3D(pos, number, W, BoxSize, threads=1):
     """MAS_library.pyx:1377"""
     _c3d("PCS", pos, number, BoxSize, W)
+
+
+def CIC_interp(density, BoxSize, pos, den):
+    """Trilinear (CIC) interpolation of ``density`` (dims^3 float32) at
+    ``pos`` ((n, 3) float32) into ``den`` ((n,) float32), in place
+    (MAS_library.pyx:558-599)."""
+    require_dtype(density, "float32", "density")
+    require_dtype(pos, "float32", "pos")
+    require_dtype(den, "float32", "den")
+    if density.ndim != 3 or pos.ndim != 2 or den.ndim != 1:
+        raise ValueError("density must be 3D, pos 2D and den 1D")
+    n = int(pos.shape[0])
+    dims = int(density.shape[0])
+    if int(den.shape[0]) < n:
+        raise ValueError("den has %d entries for %d positions" % (int(den.shape[0]), n))
+    cuda = [is_cuda_tensor(x) for x in (density, pos, den)]
+    if all(cuda):
+        ctx = _native.context(den.device.index or 0)
+        g, p = density.contiguous(), pos.contiguous()
+        out = den if den.is_contiguous() else den.contiguous()
+        torch_sync(out)
+        ctx.check(ctx.lib.pyl_cic_interp(ctx.ptr, dev_ptr(g), dims, ctypes.c_float(BoxSize),
+                                         dev_ptr(p), n, dev_ptr(out), _native.PYL_DEVICE_PTRS))
+        ctx.synchronize()
+        if out is not den:
+            den.copy_(out)
+        return
+    if any(cuda):
+        raise ValueError("density, pos and den must be all host arrays or all CUDA tensors")
+    ctx = _native.context(0)
+    g = np.ascontiguousarray(density.cpu().numpy() if is_tensor(density) else density)
+    p = np.ascontiguousarray(pos.cpu().numpy() if is_tensor(pos) else pos)
+    out = den if (isinstance(den, np.ndarray) and den.flags.c_contiguous) else np.empty(n, np.float32)
+    ctx.check(ctx.lib.pyl_cic_interp(ctx.ptr, host_ptr(g), dims, ctypes.c_float(BoxSize),
+                                     host_ptr(p), n, host_ptr(out), 0))
+    if out is not den:
+        den[:n] = out

@@ -43,6 +43,8 @@ EXPORTS = (
     "pyl_fft_r2c", "pyl_fft_c2r", "pyl_pk_sizes", "pyl_pk", "pyl_pk_particles",
     "pyl_ctx_set_timing", "pyl_ctx_stage_times", "pyl_stage_name", "pyl_pk_noalloc",
     "pyl_pk_particles_enqueue", "pyl_pk_query", "pyl_pk_collect",
+    "pyl_correct_mas", "pyl_fft2_r2c", "pyl_fft2_c2r", "pyl_pk_plane", "pyl_cic_interp",
+    "pyl_xpk",
 )
 
 
@@ -56,6 +58,12 @@ class PkOut(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in (
         "k3D", "Pk", "Nmodes3D", "k1D", "Pk1D", "Nmodes1D", "kpar", "kper",
         "Pk2D", "Nmodes2D", "Pkphase")]
+
+
+class XPkOut(ctypes.Structure):
+    names = ("k3D", "Pk", "XPk", "Nmodes3D", "k1D", "Pk1D", "PkX1D", "Nmodes1D",
+             "kpar", "kper", "Pk2D", "PkX2D", "Nmodes2D")
+    _fields_ = [(name, ctypes.c_void_p) for name in names]
 
 
 _lib = None
@@ -104,6 +112,12 @@ def load():
             "pyl_pk_particles_enqueue": [vp, vp, i64, vp, i32, f32, i32, i32, i32, i32, i32],
             "pyl_pk_query": [vp],
             "pyl_pk_collect": [vp, ctypes.POINTER(PkOut), i32],
+            "pyl_correct_mas": [vp, vp, vp, i32, i32, i32],
+            "pyl_fft2_r2c": [vp, vp, vp, i32, i32],
+            "pyl_fft2_c2r": [vp, vp, vp, i32, i32],
+            "pyl_pk_plane": [vp, vp, i32, f64, i32, vp, vp, vp, i32],
+            "pyl_cic_interp": [vp, vp, i32, f32, vp, i64, vp, i32],
+            "pyl_xpk": [vp, vp, i32, i32, f64, i32, vp, ctypes.POINTER(XPkOut), i32],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)

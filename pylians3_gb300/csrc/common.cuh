@@ -179,6 +179,8 @@ int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n
 // in-place c2c along axis 0 (x) or 1 (y) of an (n, n, h) complex array whose
 // rows have stride rs >= h
 int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int dir);
+// in-place c2c along axis 0 of an (n, rs) complex plane (its first h columns)
+int fft_plane_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int dir);
 
 // fft_reg.cu: lengths 2^k (16..4096) and 3*2^k (48..3072)
 bool reg_supported(int n);

@@ -171,6 +171,31 @@ int fft_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n
     return PYL_OK;
 }
 
+int fft_plane_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int dir) {
+    int st = PYL_OK;
+    const FftPlan *P = fft_plan(ctx, n, &st);
+    if (!P) return st;
+    if (reg_supported(n)) return pow2_cols(ctx, data, n, h, rs, 0, 1, dir, P->d_tw);
+    if (rs != h) return fail(ctx, PYL_ERR_UNSUPPORTED, "padded rows need 2^k or 3*2^k");
+    int B = 16;
+    while (B > 1 && sizeof(float2) * (size_t)B * (n + 1) > kLineBudget) B >>= 1;
+    while (B > 1 && B / 2 >= h) B >>= 1;
+    const size_t smem = sizeof(float2) * ((size_t)n + 2 * (size_t)B * (n + 1));
+    if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "FFT length too large");
+    // one outer index: axis 1 of a (1, n, h) array is axis 0 of the plane
+    dim3 grid((h + B - 1) / B, 1);
+    if (dir < 0) {
+        if ((st = set_smem(ctx, k_axis_c2c<-1>, smem))) return st;
+        k_axis_c2c<-1><<<grid, kThreads, smem, ctx->stream>>>(data, h, 1, P->desc, P->d_tw, B);
+    } else {
+        if ((st = set_smem(ctx, k_axis_c2c<+1>, smem))) return st;
+        k_axis_c2c<+1><<<grid, kThreads, smem, ctx->stream>>>(data, h, 1, P->desc, P->d_tw, B);
+    }
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    return PYL_OK;
+}
+
 int fft_axis_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int axis, int dir) {
     int st = PYL_OK;
     const FftPlan *P = fft_plan(ctx, n, &st);

@@ -22,6 +22,13 @@ inputs) at run time.  Inputs are small and seeded:
   pipeline_golden.npz  The canonical caller in miniature (Pk_snapshot.py:81-89):
                        uniform positions -> MA CIC -> delta/mean-1 -> Pk,
                        dims 32, axis 0.
+  next_golden.npz      The rows around the spectrum: correct_MAS (dims 16, 17;
+                       CIC/TSC/PCS/None) [Pk_library.pyx:1882-1939], Pk_plane
+                       (grid 16, 17, 32; NGP/CIC/PCS/None) [:435-511], XPk of
+                       three fields with mixed schemes (dims 16, 17; axis 0, 2)
+                       [:529-735], CIC_interp (dims 16, 17; uniform and edge
+                       positions) [MAS_library.pyx:558-599].
+                       `python tests/golden/make_golden.py next` writes only it.
 The reference's Pk calls pyFFTW; here it runs on the scipy.fft stand-in in
 oracle/pyfftw_shim (float32 in, complex64 out, as FFTW3f).
 """
@@ -109,10 +116,60 @@ def main():
     for k in PK_KEYS:
         out[k] = np.asarray(getattr(r, k))
     np.savez_compressed(os.path.join(HERE, "pipeline_golden.npz"), **out)
+    next_rows(MASL, PKL)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
+XPK_KEYS = ("k3D", "Pk", "XPk", "Nmodes3D", "k1D", "Pk1D", "PkX1D", "Nmodes1D", "kpar",
+            "kper", "Pk2D", "PkX2D", "Nmodes2D")
+
+
+def next_rows(MASL, PKL):
+    rng = np.random.default_rng(20261204)
+    out = {}
+    # correct_MAS
+    for dims in (16, 17):
+        delta = rng.standard_normal((dims,) * 3).astype(np.float32)
+        out["cm_delta_d%d" % dims] = delta
+        for MAS in ("CIC", "TSC", "PCS", "None"):
+            out["cm_out_d%d_%s" % (dims, MAS)] = np.asarray(
+                PKL.correct_MAS(delta, BOX, MAS=MAS, threads=1))
+    # Pk_plane
+    for grid in (16, 17, 32):
+        delta = rng.standard_normal((grid, grid)).astype(np.float32)
+        out["pp_delta_g%d" % grid] = delta
+        for MAS in ("NGP", "CIC", "PCS", "None"):
+            r = PKL.Pk_plane(delta, BOX, MAS=MAS, threads=1, verbose=False)
+            for k in ("k", "Pk", "Nmodes"):
+                out["pp_%s_g%d_%s" % (k, grid, MAS)] = np.asarray(getattr(r, k))
+    # XPk: three fields, the third correlated with the first
+    for dims in (16, 17):
+        a = rng.standard_normal((dims,) * 3).astype(np.float32)
+        b = rng.standard_normal((dims,) * 3).astype(np.float32)
+        c = (0.5 * a + 0.5 * rng.standard_normal((dims,) * 3)).astype(np.float32)
+        for i, f in enumerate((a, b, c)):
+            out["xp_delta%d_d%d" % (i, dims)] = f
+        for axis in (0, 2):
+            r = PKL.XPk([a, b, c], BOX, axis=axis, MAS=["CIC", "PCS", "CIC"], threads=1)
+            for k in XPK_KEYS:
+                out["xp_%s_d%d_a%d" % (k, dims, axis)] = np.asarray(getattr(r, k))
+    # CIC_interp
+    for dims in (16, 17):
+        grid = rng.standard_normal((dims,) * 3).astype(np.float32)
+        pos = (rng.random((4000, 3), dtype=np.float32) * np.float32(BOX))
+        pos = np.concatenate([pos, edge_positions(dims, 3)]).astype(np.float32)
+        den = np.zeros(len(pos), np.float32)
+        MASL.CIC_interp(grid, BOX, pos, den)
+        out["ci_grid_d%d" % dims] = grid
+        out["ci_pos_d%d" % dims] = pos
+        out["ci_den_d%d" % dims] = den
+    np.savez_compressed(os.path.join(HERE, "next_golden.npz"), **out)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "next":
+        next_rows(*build_ref.load())
+    else:
+        main()

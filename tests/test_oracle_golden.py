@@ -6,6 +6,8 @@ must reproduce them: mode counts and k-bins exactly, grids to float32
 rounding (the reference was built with -ffast-math, which contracts some
 multiply-adds), spectra to float64 rounding.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -123,3 +125,52 @@ def test_f64_omp_deposit_matches_serial(oracle):
             a = oracle.MA_f64(pos, 20, BOX, MAS, W=w)
             b = oracle.MA_f64(pos, 20, BOX, MAS, W=w, threads=2)
             assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+
+
+# ------------------------------------------------------------- next rows
+@pytest.fixture(scope="module")
+def nxt():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "next_golden.npz"))
+
+
+@pytest.mark.parametrize("dims", [16, 17])
+@pytest.mark.parametrize("MAS", ["CIC", "TSC", "PCS", "None"])
+def test_correct_mas_matches_reference(nxt, oracle, dims, MAS):
+    got = oracle.correct_MAS(nxt["cm_delta_d%d" % dims], BOX, MAS=MAS)
+    want = nxt["cm_out_d%d_%s" % (dims, MAS)]
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+
+
+@pytest.mark.parametrize("grid", [16, 17, 32])
+@pytest.mark.parametrize("MAS", ["NGP", "CIC", "PCS", "None"])
+def test_pk_plane_matches_reference(nxt, oracle, grid, MAS):
+    r = oracle.Pk_plane(nxt["pp_delta_g%d" % grid], BOX, MAS=MAS)
+    np.testing.assert_array_equal(r.Nmodes, nxt["pp_Nmodes_g%d_%s" % (grid, MAS)])
+    np.testing.assert_allclose(r.k, nxt["pp_k_g%d_%s" % (grid, MAS)], rtol=1e-12)
+    np.testing.assert_allclose(r.Pk, nxt["pp_Pk_g%d_%s" % (grid, MAS)], rtol=1e-6)
+
+
+@pytest.mark.parametrize("dims", [16, 17])
+@pytest.mark.parametrize("axis", [0, 2])
+def test_xpk_matches_reference(nxt, oracle, dims, axis):
+    fields = [nxt["xp_delta%d_d%d" % (i, dims)] for i in range(3)]
+    r = oracle.XPk(fields, BOX, axis=axis, MAS=["CIC", "PCS", "CIC"])
+    for key in ("Nmodes3D", "Nmodes1D", "Nmodes2D"):
+        np.testing.assert_array_equal(getattr(r, key), nxt["xp_%s_d%d_a%d" % (key, dims, axis)])
+    for key in ("k3D", "k1D", "kpar", "kper"):
+        np.testing.assert_allclose(getattr(r, key), nxt["xp_%s_d%d_a%d" % (key, dims, axis)],
+                                   rtol=1e-12)
+    scale = np.abs(nxt["xp_Pk_d%d_a%d" % (dims, axis)]).max()
+    for key in ("Pk", "XPk", "Pk1D", "PkX1D", "Pk2D", "PkX2D"):
+        want = nxt["xp_%s_d%d_a%d" % (key, dims, axis)]
+        assert getattr(r, key).shape == want.shape, key
+        assert np.abs(getattr(r, key) - want).max() <= 1e-6 * max(scale, np.abs(want).max()), key
+
+
+@pytest.mark.parametrize("dims", [16, 17])
+def test_cic_interp_matches_reference(nxt, oracle, dims):
+    pos = nxt["ci_pos_d%d" % dims]
+    den = np.zeros(len(pos), np.float32)
+    oracle.CIC_interp(nxt["ci_grid_d%d" % dims], BOX, pos, den)
+    want = nxt["ci_den_d%d" % dims]
+    assert np.abs(den - want).max() <= 1e-6 * np.abs(want).max()
