@@ -237,6 +237,13 @@ int pyl_pk_plane(pyl_ctx *ctx, const float *delta, int grid, double BoxSize,
 int pyl_cic_interp(pyl_ctx *ctx, const float *density, int dims, float BoxSize,
                    const float *pos, int64_t n, float *den, int flags);
 
+/* pos_redshift_space (library/redshift_space_library/
+ * redshift_space_library.pyx:29-50), in place on the (n, 3) positions:
+ * pos[:, axis] += vel[:, axis] (1 + redshift) / Hubble, wrapped into
+ * [0, BoxSize].                                                            */
+int pyl_rsd(pyl_ctx *ctx, float *pos, const float *vel, int64_t n, float BoxSize,
+            float Hubble, float redshift, int axis, int flags);
+
 /* class XPk (Pk_library.pyx:529-735): auto- and cross-spectra of nfields
  * (1..8) float32 fields of the same dims^3 grid, mas[i] the window of field
  * i.  With X = nfields (nfields - 1) / 2 pairs (i < j in row order), the

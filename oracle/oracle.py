@@ -472,3 +472,18 @@ def CIC_interp(density, BoxSize, pos, den):
         t = g[ix[:, 0], iy[:, 1], iz[:, 2]] * a[:, 0] * b[:, 1] * cc[:, 2]
         s = t if s is None else (s + t).astype(np.float32)
     den[:len(s)] = s
+
+
+def pos_redshift_space(pos, vel, BoxSize, Hubble, redshift, axis):
+    """Restatement of pos_redshift_space (redshift_space_library.pyx:29-50),
+    in place, float32 steps as written."""
+    factor = np.float32((1.0 + float(np.float32(redshift))) / float(np.float32(Hubble)))
+    box = np.float32(BoxSize)
+    p = (pos[:, axis] + vel[:, axis] * factor).astype(np.float32)
+    neg = p < 0
+    while neg.any():
+        p[neg] = p[neg] + box
+        neg = p < 0
+    big = p > box
+    p[big] = np.fmod(p[big], box)
+    pos[:, axis] = p

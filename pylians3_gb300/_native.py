@@ -44,7 +44,7 @@ EXPORTS = (
     "pyl_ctx_set_timing", "pyl_ctx_stage_times", "pyl_stage_name", "pyl_pk_noalloc",
     "pyl_pk_particles_enqueue", "pyl_pk_query", "pyl_pk_collect",
     "pyl_correct_mas", "pyl_fft2_r2c", "pyl_fft2_c2r", "pyl_pk_plane", "pyl_cic_interp",
-    "pyl_xpk",
+    "pyl_xpk", "pyl_rsd",
 )
 
 
@@ -118,6 +118,7 @@ def load():
             "pyl_pk_plane": [vp, vp, i32, f64, i32, vp, vp, vp, i32],
             "pyl_cic_interp": [vp, vp, i32, f32, vp, i64, vp, i32],
             "pyl_xpk": [vp, vp, i32, i32, f64, i32, vp, ctypes.POINTER(XPkOut), i32],
+            "pyl_rsd": [vp, vp, vp, i64, f32, f32, f32, i32, i32],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)

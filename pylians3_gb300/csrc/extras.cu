@@ -4,6 +4,8 @@
 //   Pk_plane     Pk_library.pyx:435-511    (2D r2c, window, |k| bins) with
 //                FFT2Dr_f / IFFT2Dr_f       Pk_library.pyx:181-228
 //   CIC_interp   MAS_library.pyx:558-599   (gather of a grid at positions)
+//   pos_redshift_space  redshift_space_library.pyx:29-50 (the RSD shift of
+//                the snapshot driver, Pk_snapshot.py:63-67)
 #include <math.h>
 #include <string.h>
 
@@ -120,6 +122,32 @@ k_cic_interp(const float *__restrict__ grid, int dims, float inv,
         s = __fadd_rn(s, t(g(iu[0], iu[1], id[2]), u[0], u[1], d[2]));
         s = __fadd_rn(s, t(g(iu[0], iu[1], iu[2]), u[0], u[1], u[2]));
         den[i] = s;
+    }
+}
+
+// pos_redshift_space (redshift_space_library.pyx:29-50): along `axis`,
+// s = r + v (1 + z) / H(z), then wrapped into [0, BoxSize]: BoxSize is added
+// while s < 0 (particles that crossed the box several times), and s above
+// BoxSize is replaced by fmod(s, BoxSize); float32 steps as written (no
+// fused multiply-add).  The loop of additions is bounded: past 1024 box
+// lengths below 0 the wrap is done with fmod instead.
+__global__ void __launch_bounds__(kThreads)
+k_rsd(float *__restrict__ pos, const float *__restrict__ vel, long long n, float box,
+      float factor, int axis) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float p = __fadd_rn(pos[3 * i + axis], __fmul_rn(vel[3 * i + axis], factor));
+        int it = 0;
+        while (p < 0.f && it < 1024) {
+            p = __fadd_rn(p, box);
+            ++it;
+        }
+        if (p < 0.f) {
+            p = fmodf(p, box);
+            if (p < 0.f) p = __fadd_rn(p, box);
+        }
+        if (p > box) p = fmodf(p, box);
+        pos[3 * i + axis] = p;
     }
 }
 
@@ -337,6 +365,37 @@ int pyl_pk_plane(pyl_ctx *ctx, const float *delta, int grid, double BoxSize, int
         if (k) k[b - 1] = (ksum[b] / N[b]) * kF;
         if (Pk) Pk[b - 1] = (sums[b] / N[b]) * unit;
         if (Nmodes) Nmodes[b - 1] = N[b];
+    }
+    return PYL_OK;
+}
+
+int pyl_rsd(pyl_ctx *ctx, float *pos, const float *vel, int64_t n, float BoxSize, float Hubble,
+            float redshift, int axis, int flags) {
+    if (!ctx) return PYL_ERR_ARG;
+    if (n < 0 || axis < 0 || axis > 2 || (n > 0 && (!pos || !vel)))
+        return fail(ctx, PYL_ERR_ARG, "bad pos_redshift_space arguments");
+    if (n == 0) return PYL_OK;
+    PYL_CUDA(ctx, cudaSetDevice(ctx->device));
+    const bool dev = flags & PYL_DEVICE_PTRS;
+    int st = PYL_OK;
+    float *dp = pos;
+    if (!dev) {
+        dp = (float *)ws_get(ctx, "rsd_pos", sizeof(float) * 3 * (size_t)n, &st);
+        if (!dp) return st;
+        PYL_CUDA(ctx, cudaMemcpyAsync(dp, pos, sizeof(float) * 3 * (size_t)n,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    }
+    const float *dv = stage_in(ctx, vel, (size_t)n * 3, dev, "rsd_vel", &st);
+    if (!dv) return st;
+    // factor = (1.0 + redshift) / Hubble in double, stored as float (:34)
+    const float factor = (float)((1.0 + (double)redshift) / (double)Hubble);
+    k_rsd<<<grid_for(n), kThreads, 0, ctx->stream>>>(dp, dv, n, BoxSize, factor, axis);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    if (!dev) {
+        PYL_CUDA(ctx, cudaMemcpyAsync(pos, dp, sizeof(float) * 3 * (size_t)n,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+        return status_check(ctx);
     }
     return PYL_OK;
 }
