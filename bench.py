@@ -89,6 +89,28 @@ def dist_env():
     return rank, world, local
 
 
+# Replicas: every rank runs its own spectra on its own seeded particles; no
+# data crosses ranks.  The only collective is the max of the per-rank times.
+def replica_seed(rank):
+    return 1234 + rank
+
+
+def max_over_ranks(value, world, device):
+    """Max over the ranks of a per-rank time (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, steps, seconds):
+    """Whole-job spectra/s: every rank's steps over the slowest rank's time."""
+    return world * steps / seconds
+
+
 # ------------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
@@ -273,9 +295,9 @@ def run_ours(a):
     ctx = _native.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     if a.positions == "uniform":
-        pos = synth.uniform(a.particles, BOX, seed=1234 + rank)
+        pos = synth.uniform(a.particles, BOX, seed=replica_seed(rank))
     else:
-        pos = synth.zeldovich(a.dims, BOX, sigma=3.0, seed=1234 + rank)
+        pos = synth.zeldovich(a.dims, BOX, sigma=3.0, seed=replica_seed(rank))
         a.particles = pos.shape[0]
     torch.cuda.synchronize()
     out = _Outputs(a.dims, 0)
@@ -319,14 +341,9 @@ def run_ours(a):
     stages = ctx.stage_times(reset=True)
     ctx.set_timing(False)
     barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     ms_step = ms / a.steps
-    value = world * a.steps / (ms / 1e3)
+    value = job_rate(world, a.steps, ms / 1e3)
 
     # ---- roofline of the dominant kernel
     peak, peak_kind = peaks()
@@ -356,14 +373,9 @@ def run_ours(a):
         for _ in range(a.steps):
             P.power_spectrum(host, a.dims, BOX, a.mas, axis=a.axis, ctx=ctx)
         t1 = time.perf_counter()
-        sec = t1 - t0
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([sec], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            sec = float(t.item())
+        sec = max_over_ranks(t1 - t0, world, "cuda")
         kmax = _native.pk_sizes(a.dims)[0]
-        e2e = {"value": world * a.steps / sec, "unit": UNIT,
+        e2e = {"value": job_rate(world, a.steps, sec), "unit": UNIT,
                "h2d_bytes_per_step": a.particles * 12,
                "d2h_bytes_per_step": 8 * (5 * (kmax + 1)),
                "ms_per_step": sec / a.steps * 1e3}
