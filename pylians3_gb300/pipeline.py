@@ -77,3 +77,69 @@ def power_spectrum(pos, dims, BoxSize, MAS="CIC", axis=2, W=None, window=None,
     res = Spectrum()
     out.assign(res)
     return res
+
+
+_pools: dict = {}
+
+
+def _pool(device, depth):
+    """Contexts (each with its own stream and workspaces) kept per device."""
+    key = (device, depth)
+    if key not in _pools:
+        _pools[key] = [_native.Context(device) for _ in range(depth)]
+    return _pools[key]
+
+
+def power_spectra(pos_sets, dims, BoxSize, MAS="CIC", axis=2, W_sets=None, window=None,
+                  what=0, deposit="auto", depth=2, device=0):
+    """Spectra of several particle sets (the power_spectrum path for each),
+    with up to ``depth`` sets in flight on separate contexts: the copy of one
+    set's host positions to the device overlaps the computation of the set
+    before it (the copy engine and the SMs work at the same time), and each
+    set's spectrum comes back as soon as it is done.  Host arrays should be
+    in pinned memory (``pinned_empty``) for the copies to run asynchronously.
+    Returns the spectra in input order."""
+    if MAS not in _native.MAS_CODE:
+        raise ValueError("option not valid!!! (MAS must be NGP, CIC, TSC or PCS)")
+    if deposit not in DEPOSIT_FLAGS:
+        raise ValueError("deposit must be one of %s" % sorted(DEPOSIT_FLAGS))
+    win = MAS_function(MAS if window is None else window)
+    ctxs = _pool(int(device), int(depth))
+    pos_sets = list(pos_sets)
+    W_sets = [None] * len(pos_sets) if W_sets is None else list(W_sets)
+    results = [None] * len(pos_sets)
+    inflight = []     # (index, context, outputs, keep-alive)
+
+    def finish():
+        i, ctx, out, _ = inflight.pop(0)
+        _raise_or_exit(ctx, ctx.lib.pyl_pk_collect(ctx.ptr, ctypes.byref(out.struct), -1))
+        res = Spectrum()
+        out.assign(res)
+        results[i] = res
+
+    for i, (pos, W) in enumerate(zip(pos_sets, W_sets)):
+        require_dtype(pos, "float32", "pos")
+        if pos.ndim != 2 or int(pos.shape[1]) != 3:
+            raise ValueError("pos must be (n, 3)")
+        n = int(pos.shape[0])
+        if len(inflight) == len(ctxs):
+            finish()
+        ctx = ctxs[i % len(ctxs)]
+        out = _Outputs(int(dims), what)
+        if is_cuda_tensor(pos):
+            p = pos.contiguous()
+            w = None if W is None else W.contiguous()
+            torch_sync(p)
+            pp, wp, flags = dev_ptr(p), (dev_ptr(w) if w is not None else None), _native.PYL_DEVICE_PTRS
+        else:
+            p = np.ascontiguousarray(pos)
+            w = None if W is None else np.ascontiguousarray(W, np.float32)
+            pp, wp, flags = host_ptr(p), (host_ptr(w) if w is not None else None), 0
+        rc = ctx.lib.pyl_pk_particles_enqueue(ctx.ptr, pp, n, wp, int(dims), ctypes.c_float(BoxSize),
+                                              _native.MAS_CODE[MAS], int(axis), win, int(what),
+                                              flags | DEPOSIT_FLAGS[deposit])
+        _raise_or_exit(ctx, rc)
+        inflight.append((i, ctx, out, (p, w)))
+    while inflight:
+        finish()
+    return results

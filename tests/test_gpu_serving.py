@@ -107,3 +107,25 @@ def test_server_budget(env):
     with pytest.raises(native.PylError):
         srv.submit(make_pos(torch, 1 << 22, 8), 128, BOX, "CIC")
     srv.close()
+
+
+def test_power_spectra_matches_single_calls(env):
+    """The pipelined multi-set call returns, in order, what power_spectrum
+    returns for each set (host pinned and device inputs mixed)."""
+    torch, native, P = env
+    sets = []
+    for i, dims in enumerate((64, 96, 64, 128)):
+        pos = make_pos(torch, dims ** 3 * 2, 500 + i)
+        if i % 2 == 0:
+            host = P.pinned_empty(tuple(pos.shape))
+            host[...] = pos.cpu().numpy()
+            pos = host
+        sets.append((pos, dims))
+    for dims in {d for _, d in sets}:
+        group = [p for p, d in sets if d == dims]
+        many = P.power_spectra(group, dims, BOX, "TSC", axis=1)
+        for p, m in zip(group, many):
+            one = P.power_spectrum(p, dims, BOX, "TSC", axis=1)
+            assert np.array_equal(one.Nmodes3D, m.Nmodes3D)
+            err = np.abs(m.Pk - one.Pk).max(axis=1) / np.abs(one.Pk[:, 0])
+            assert err[:dims // 2 + 1].max() <= TOL_PK
