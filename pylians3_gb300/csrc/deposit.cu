@@ -264,8 +264,24 @@ struct TileGeom {
     int ncoarse;         // coarse buckets = ceil(ntiles / F)
 };
 
-constexpr int KP = 1024;          // particles staged per partition step
-constexpr int kPartThreads = 256; // >= kMaxKeys (one scan value per thread)
+// Partition shape (compile-time; the defaults are the measured best):
+// particles staged per chunk, threads per CTA (>= kMaxKeys: one scan value
+// per thread), resident CTAs per SM the registers are sized for.
+#ifndef PYL_PART_KP
+#define PYL_PART_KP 1024
+#endif
+#ifndef PYL_PART_THREADS
+#define PYL_PART_THREADS 256
+#endif
+#ifndef PYL_PART_MINB
+#define PYL_PART_MINB 4
+#endif
+#ifndef PYL_PART_WRITE
+#define PYL_PART_WRITE 1
+#endif
+constexpr int KP = PYL_PART_KP;
+constexpr int kPartThreads = PYL_PART_THREADS;
+static_assert(KP % 4 == 0, "bulk copies move whole 16-byte groups");
 constexpr int kMaxKeys = 256;     // buckets of one partition step
 constexpr unsigned kItemCap = 65536;  // particles per deposit work item
 
@@ -384,7 +400,7 @@ __global__ void k_items(const unsigned *__restrict__ nchunk_ex, const unsigned *
 // histogram, one global atomic per key on that key's cursor, a shared
 // counting sort, then each key's run is written out contiguously.
 template <int MAS, bool HAS_W, bool FINE>
-__global__ void __launch_bounds__(kPartThreads, 4)
+__global__ void __launch_bounds__(kPartThreads, PYL_PART_MINB)
 k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             float *__restrict__ dst, float *__restrict__ dstw, long long n, float inv,
             TileGeom g, unsigned *__restrict__ cursor, const unsigned *__restrict__ start,
@@ -498,11 +514,15 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             }
             __syncthreads();
             const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
+            // Reserve the key's run in the destination now; the write-out is
+            // the first to need it, so the atomic's round trip overlaps the
+            // scan and the shared counting sort.
+            unsigned my_base = 0u;
+            if (hv) my_base = atomicAdd(&cursor[keybase + threadIdx.x], hv);
             const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
             if (threadIdx.x < nkeys) {
                 loff[threadIdx.x] = ex;
                 lcur[threadIdx.x] = ex;
-                gbase[threadIdx.x] = hv ? atomicAdd(&cursor[keybase + threadIdx.x], hv) : 0u;
             }
             __syncthreads();
             for (int i = threadIdx.x; i < cs; i += blockDim.x) {
@@ -515,8 +535,22 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
                 if (HAS_W) sw2[r] = sw[o + i];
                 skey2[r] = (unsigned short)key;
             }
+            if (threadIdx.x < nkeys) gbase[threadIdx.x] = my_base;
             __syncthreads();
             // key runs are contiguous both here and in the destination
+#if PYL_PART_WRITE == 1
+            // one particle per thread: consecutive threads hold consecutive
+            // slots of a run, so each of the three stores covers one span
+            for (int e = threadIdx.x; e < cs; e += blockDim.x) {
+                const int key = skey2[e];
+                const size_t d = (size_t)gbase[key] + (e - loff[key]);
+                const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
+                dst[3 * d] = x;
+                dst[3 * d + 1] = y;
+                dst[3 * d + 2] = z;
+                if (HAS_W) dstw[d] = sw2[e];
+            }
+#else
             for (int j = threadIdx.x; j < 3 * cs; j += blockDim.x) {
                 const int e = j / 3;
                 const int key = skey2[e];
@@ -529,6 +563,7 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
                     dstw[(size_t)gbase[key] + (e - loff[key])] = sw2[e];
                 }
             }
+#endif
             __syncthreads();
             seg0 = seg1;
         }
