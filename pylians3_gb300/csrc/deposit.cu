@@ -23,6 +23,7 @@
 // index 0 and weight 1 for every tap, so a particle is deposited 2/3/4 times
 // onto the same plane for CIC/TSC/PCS (and renormalised by the caller).
 #include <algorithm>
+#include <type_traits>
 
 #include "async_copy.cuh"
 #include "deposit_common.cuh"
@@ -623,23 +624,27 @@ struct TapBound {
 //     a[j] <- sum of a[k] for k in [j - HI, j + LO]   (0 outside the line),
 // the cells whose taps can reach cell j (taps lie at home + [-LO, HI]).
 // The last LO + HI inputs are kept in registers while the line is rewritten.
-template <int LO, int HI>
-__device__ __forceinline__ int box_line(int *a, int n, int st, bool write) {
+// Counts (int) or sums of |W| (float, then each window is summed afresh so
+// that no rounding drift builds up along the line).
+template <int LO, int HI, typename T>
+__device__ __forceinline__ T box_line(T *a, int n, int st, bool write) {
     constexpr int R = LO + HI + 1;
-    int r[R];
+    T r[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) r[q] = 0;
-    int sum = 0, best = 0;
+    for (int q = 0; q < R; ++q) r[q] = T(0);
+    T best = T(0);
     for (int k = 0; k < n + LO; ++k) {
-        const int x = k < n ? a[k * st] : 0;
-        sum += x - r[0];
+        const T x = k < n ? a[k * st] : T(0);
 #pragma unroll
         for (int q = 0; q + 1 < R; ++q) r[q] = r[q + 1];
         r[R - 1] = x;
+        T sum = r[0];
+#pragma unroll
+        for (int q = 1; q < R; ++q) sum += r[q];
         const int j = k - LO;
         if (j >= 0) {
             if (write) a[j * st] = sum;
-            best = max(best, sum);
+            best = best > sum ? best : sum;
         }
     }
     return best;
@@ -648,12 +653,14 @@ __device__ __forceinline__ int box_line(int *a, int n, int st, bool write) {
 // Deposit: work items (tile, chunk) over a persistent grid; shared
 // footprint, shared atomics, then a global flush of the footprint.
 //
-// FIXED (unit weights): the footprint is accumulated in 32-bit integers,
-// each tap rounded to a fixed point of scale 2^e.  A first pass over the
-// item's particles histograms their home cells; a box sum of the histogram
-// over the stencil's reach gives, for every footprint cell, how many
-// particles can reach it, so no cell can exceed WMAX times the largest box
-// sum, and 2^e is the largest power of two keeping that bound under 2^30.
+// FIXED: the footprint is accumulated in 32-bit integers, each tap rounded
+// to a fixed point of scale 2^e.  A first pass over the item's particles
+// histograms their home cells (counts, or sums of |W| for weighted
+// particles); a box sum of the histogram over the stencil's reach gives, for
+// every footprint cell, how much mass can reach it, so no cell can exceed
+// WMAX times the largest box sum, and 2^e is the largest power of two keeping
+// that bound under 2^30.  An item whose bound is not finite (weights of inf
+// or NaN) falls back to float atomics.
 // Integer shared atomics run at about twice the rate of float ones, and the
 // sums are exact (independent of the order of the atomics); the flush
 // converts each cell once (int -> float rounding, then an exact scaling by
@@ -672,12 +679,11 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                float *__restrict__ grid, int vec4, float *__restrict__ glo) {
     constexpr bool FIXED = ACC == kAccFixed;
     constexpr bool COMP = ACC == kAccComp;
-    static_assert(!(FIXED && HAS_W), "fixed-point accumulation is for unit weights");
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
     extern __shared__ float s_reg[];
     int *s_int = reinterpret_cast<int *>(s_reg);
-    __shared__ int s_max[32];
+    __shared__ float s_max[32];
     const int RX = g.RX, RY = g.RY, RZ = g.RZ;
     const int cells = RX * RY * RZ;
     const unsigned total = *nitems;
@@ -691,56 +697,73 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         const long long p1 = min((long long)start[t + 1], p0 + (long long)kItemCap);
         __syncthreads();
         float scale = 1.f, inv_scale = 1.f;
+        bool fixed = FIXED;   // this item in fixed point
         if (FIXED) {
-            // ---- home-cell occupancy of the item, its maximum, the scale
-            auto occupy = [&](float x, float y, float z) {
+            // ---- home-cell occupancy (or |W| per home cell), its box sums,
+            // their maximum, the scale
+            auto occupy = [&](float x, float y, float z, float w) {
                 const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
                 const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
                 const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
-                atomicAdd(&s_int[((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ +
-                                 (hz - oz + S::LO)],
-                          1);
+                const int c = ((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ + (hz - oz + S::LO);
+                if (HAS_W) atomicAdd(&s_reg[c], fabsf(w));
+                else atomicAdd(&s_int[c], 1);
             };
             // two particles per thread and step, both loaded first
             for (long long i = p0 + threadIdx.x; i < p1; i += 2 * blockDim.x) {
                 const long long i2 = i + blockDim.x;
                 const float x = __ldg(spos + 3 * i), y = __ldg(spos + 3 * i + 1),
                             z = __ldg(spos + 3 * i + 2);
-                float x2 = 0.f, y2 = 0.f, z2 = 0.f;
+                const float w = HAS_W ? __ldg(sw + i) : 1.f;
+                float x2 = 0.f, y2 = 0.f, z2 = 0.f, w2 = 1.f;
                 if (i2 < p1) {
                     x2 = __ldg(spos + 3 * i2);
                     y2 = __ldg(spos + 3 * i2 + 1);
                     z2 = __ldg(spos + 3 * i2 + 2);
+                    if (HAS_W) w2 = __ldg(sw + i2);
                 }
-                occupy(x, y, z);
-                if (i2 < p1) occupy(x2, y2, z2);
+                occupy(x, y, z, w);
+                if (i2 < p1) occupy(x2, y2, z2, w2);
             }
             __syncthreads();
             // separable box sums: z lines, y lines, then x lines (max only)
+            using T = typename std::conditional<HAS_W, float, int>::type;
+            T *hs = reinterpret_cast<T *>(s_reg);
             for (int l = threadIdx.x; l < RX * RY; l += blockDim.x)
-                box_line<S::LO, S::HI>(s_int + l * RZ, RZ, 1, true);
+                box_line<S::LO, S::HI, T>(hs + l * RZ, RZ, 1, true);
             __syncthreads();
             for (int l = threadIdx.x; l < RX * RZ; l += blockDim.x)
-                box_line<S::LO, S::HI>(s_int + (l / RZ) * RY * RZ + (l % RZ), RY, RZ, true);
+                box_line<S::LO, S::HI, T>(hs + (l / RZ) * RY * RZ + (l % RZ), RY, RZ, true);
             __syncthreads();
-            int m = 0;
-            for (int l = threadIdx.x; l < RY * RZ; l += blockDim.x)
-                m = max(m, box_line<S::LO, S::HI>(s_int + l, RX, RY * RZ, false));
+            float m = 0.f;
+            for (int l = threadIdx.x; l < RY * RZ; l += blockDim.x) {
+                const float b = (float)box_line<S::LO, S::HI, T>(hs + l, RX, RY * RZ, false);
+                m = (b > m || b != b) ? b : m;        // keeps a NaN
+            }
             __syncthreads();
             for (int i = threadIdx.x; i < cells; i += blockDim.x) s_int[i] = 0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+            for (int o = 16; o > 0; o >>= 1) {
+                const float b = __shfl_xor_sync(0xffffffffu, m, o);
+                m = (b > m || b != b) ? b : m;
+            }
             if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
             __syncthreads();
-            m = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = max(m, s_max[w]);
-            // 2^e <= 2^30 / (WMAX * largest box sum)
-            const float bound = fmaxf(TapBound<MAS>::WMAX * (float)m, 1.f);
-            int e;
-            frexpf(bound, &e);                 // bound < 2^e
-            e = min(30 - e, 30);
-            scale = ldexpf(1.f, e);
-            inv_scale = ldexpf(1.f, -e);
+            m = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+                m = (s_max[w] > m || s_max[w] != s_max[w]) ? s_max[w] : m;
+            // 2^e <= 2^30 / (WMAX * largest box sum); float box sums of |W|
+            // get a margin for their rounding
+            const float bound =
+                fmaxf(TapBound<MAS>::WMAX * m * (HAS_W ? 1.001f : 1.f), 1.f);
+            fixed = bound < 1.0e30f;               // false for inf and NaN
+            if (fixed) {
+                int e;
+                frexpf(bound, &e);                 // bound < 2^e
+                e = min(30 - e, 30);
+                scale = ldexpf(1.f, e);
+                inv_scale = ldexpf(1.f, -e);
+            }
             __syncthreads();   // s_max is rewritten by the next item
         }
         auto deposit_one = [&](float px, float py, float pz, float wt) {
@@ -783,7 +806,8 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                     for (int q = 0; q < NT; ++q) {
                         float v = wxy * wz[q];
                         if (HAS_W) v *= wt;
-                        if (FIXED) atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
+                        if (FIXED && fixed)
+                            atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
                         else if (COMP) comp_add(s_reg + row + lz[q], s_reg + cells + row + lz[q], v);
                         else atomicAdd(s_reg + row + lz[q], v);
                     }
@@ -809,7 +833,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         __syncthreads();
         // footprint cell value as a float
         auto cell = [&](int c) {
-            return FIXED ? (float)s_int[c] * inv_scale : s_reg[c];
+            return (FIXED && fixed) ? (float)s_int[c] * inv_scale : s_reg[c];
         };
         const int d = g.dims;
         const long long dd = (long long)d * d;
@@ -1035,9 +1059,7 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         return PYL_OK;
     };
     if (acc == kAccComp) return run(k_tile_deposit<MAS, HAS_W, kAccComp>);
-    if constexpr (!HAS_W) {
-        if (acc == kAccFixed) return run(k_tile_deposit<MAS, false, kAccFixed>);
-    }
+    if (acc == kAccFixed) return run(k_tile_deposit<MAS, HAS_W, kAccFixed>);
     return run(k_tile_deposit<MAS, HAS_W, kAccFloat>);
 }
 
@@ -1047,14 +1069,14 @@ int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, f
     const TileGeom g = make_geom(dims, MAS);
     const int forced = (flags & PYL_SORT_TWO_PASS) ? kSortTwoPass
                        : (flags & PYL_SORT_FRONTIER) ? kSortFrontier : -1;
-    // Compensated if asked for; else unit weights accumulate in fixed point
-    // (NGP/CIC/TSC) unless float atomics are asked for.  PCS keeps float
+    // Compensated if asked for; else NGP/CIC/TSC accumulate in fixed point
+    // unless float atomics are asked for.  PCS keeps float
     // atomics: its deconvolution amplifies the grid's rounding noise ~5e4-fold
     // in the corner bins beyond the Nyquist wavenumber, and the coarser
     // quantization of tiles holding dense halos shows there.
     const int acc = glo ? kAccComp
-                        : (!W && MAS != PYL_MAS_PCS && !(flags & PYL_DEPOSIT_FLOAT)) ? kAccFixed
-                                                                                    : kAccFloat;
+                        : (MAS != PYL_MAS_PCS && !(flags & PYL_DEPOSIT_FLOAT)) ? kAccFixed
+                                                                              : kAccFloat;
     return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo)
              : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo);
 }
@@ -1135,13 +1157,24 @@ namespace {
 
 __global__ void __launch_bounds__(256)
 k_wsum(const float *__restrict__ W, long long n, double *__restrict__ mass) {
-    double s = 0.0;
+    // float partial sums per thread (the mass only sets the FFT shift, whose
+    // rounding the k = 0 mode corrects exactly), double across threads, one
+    // atomic per CTA
+    __shared__ double s_w[32];
+    float f = 0.f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
-        s += (double)W[i];
+        f += __ldcs(W + i);
+    double s = (double)f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(mass, s);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[w];
+        if (t != 0.0) atomicAdd(mass, t);
+    }
 }
 
 __global__ void k_shift(double *mass, long long n, int weighted, double inv_cells,
