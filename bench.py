@@ -50,7 +50,8 @@ def parse():
                     choices=["plain", "batched", "served", "precision"],
                     help="plain: the headline line; batched: 64 uneven realizations "
                          "overlapped; served: Poisson request streams")
-    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--slots", type=int, default=None,
+                    help="contexts in flight (default: 2 batched, 8 served)")
     ap.add_argument("--rates", type=float, nargs="*", default=[50.0, 200.0, 500.0])
     ap.add_argument("--seconds", type=float, default=5.0)
     ap.add_argument("--dims", type=int, default=512)
@@ -464,12 +465,13 @@ def run_batched(a):
     for r in reqs:
         P.power_spectrum(**r, ctx=ctx)
     t_seq = time.perf_counter() - t0
-    run_batch(reqs, slots=a.slots)                 # warm the slots
-    res, t_bat = run_batch(reqs, slots=a.slots)
+    slots = a.slots or 2      # measured best for this mix (1: 1152, 2: 1392, 4: 1339, 8: 1216/s)
+    run_batch(reqs, slots=slots)                   # warm the slots
+    res, t_bat = run_batch(reqs, slots=slots)
     line = {"mode": "batched", "metric": "realizations/s (64 uneven realizations)",
             "value": len(reqs) / t_bat, "unit": "spectra/s",
             "sequential_value": len(reqs) / t_seq, "speedup": t_seq / t_bat,
-            "slots": a.slots, "particles_total": int(sum(r["pos"].shape[0] for r in reqs)),
+            "slots": slots, "particles_total": int(sum(r["pos"].shape[0] for r in reqs)),
             "config": {"dims": "U{128,192,256,384}", "particles": "2^U(20,25)",
                        "positions": "uniform | zeldovich sigma U(2,5)", "W": "lognormal(0,0.5) half",
                        "mas": "U{CIC,TSC}"}}
@@ -512,7 +514,7 @@ def run_served(a):
     for rate in a.rates:
         reqs = stream(rate, a.seconds, seed=int(rate))
         row = {"rate": rate, "requests": len(reqs)}
-        for name, slots in (("served", a.slots), ("queue_only", 1)):
+        for name, slots in (("served", a.slots or 8), ("queue_only", 1)):
             srv = Server(slots=slots, hbm_budget=150e9)
             t0 = time.perf_counter()
             futs = []
@@ -531,7 +533,7 @@ def run_served(a):
                          "p99_ms": float(np.percentile(lat, 99) * 1e3), "wall_s": wall}
         results.append(row)
     line = {"mode": "served", "metric": "spectra/s and latency under Poisson arrivals",
-            "slots": a.slots, "seconds_per_rate": a.seconds, "rates": results,
+            "slots": a.slots or 8, "seconds_per_rate": a.seconds, "rates": results,
             "config": {"dims": "{64,128,256,512} p=(.3,.3,.3,.1)", "particles_per_cell": "U{1..8}",
                        "mas": "U{NGP,CIC,TSC,PCS}", "axis": "U{0,1,2}",
                        "positions": "device-resident uniform pools", "hbm_budget_gb": 150}}
