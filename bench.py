@@ -467,11 +467,22 @@ def run_batched(a):
     t_seq = time.perf_counter() - t0
     slots = a.slots or 2      # measured best for this mix (1: 1152, 2: 1392, 4: 1339, 8: 1216/s)
     run_batch(reqs, slots=slots)                   # warm the slots
-    res, t_bat = run_batch(reqs, slots=slots)
+    res, t_srv = run_batch(reqs, slots=slots)
+    # the whole batch as one CUDA graph (captured on the first call)
+    from pylians3_gb300.pipeline import spectra_batch
+    spectra_batch(reqs, ctx=ctx)
+    spectra_batch(reqs, ctx=ctx)
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        spectra_batch(reqs, ctx=ctx)
+    t_graph = (time.perf_counter() - t0) / reps
     line = {"mode": "batched", "metric": "realizations/s (64 uneven realizations)",
-            "value": len(reqs) / t_bat, "unit": "spectra/s",
-            "sequential_value": len(reqs) / t_seq, "speedup": t_seq / t_bat,
-            "slots": slots, "particles_total": int(sum(r["pos"].shape[0] for r in reqs)),
+            "value": len(reqs) / t_graph, "unit": "spectra/s",
+            "api": "pipeline.spectra_batch: the 64 requests as one CUDA graph launch",
+            "sequential_value": len(reqs) / t_seq, "speedup": t_seq / t_graph,
+            "server_value": len(reqs) / t_srv, "server_slots": slots,
+            "particles_total": int(sum(r["pos"].shape[0] for r in reqs)),
             "config": {"dims": "U{128,192,256,384}", "particles": "2^U(20,25)",
                        "positions": "uniform | zeldovich sigma U(2,5)", "W": "lognormal(0,0.5) half",
                        "mas": "U{CIC,TSC}"}}

@@ -63,6 +63,9 @@ enum { PYL_MAS_NONE = 0, PYL_MAS_NGP = 1, PYL_MAS_CIC = 2, PYL_MAS_TSC = 3,
  * and the tile's sums are then exact.  This flag keeps float32 shared
  * atomics instead (always used for PCS and for weighted particles).        */
 #define PYL_DEPOSIT_FLOAT  0x40
+/* pyl_pk_batch: issue the requests directly instead of through the cached
+ * CUDA graph (the same work, launch by launch).                           */
+#define PYL_NO_GRAPH       0x80
 
 /* Which Pk outputs to compute (bit mask); the 3D multipoles always are.   */
 #define PYL_PK_3D     0x00
@@ -207,6 +210,28 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms);
  * (create the context with a caller stream so that it makes no stream).    */
 int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double BoxSize,
                    int axis, int mas, int what, pyl_pk_out *out);
+
+/* One particles -> spectrum request (the arguments of pyl_pk_particles). */
+typedef struct {
+    const float *pos;   /* (n, 3) positions                                */
+    int64_t n;
+    const float *W;     /* (n,) weights or NULL                             */
+    int dims;
+    float BoxSize;
+    int mas_deposit, axis, mas_window, what;
+} pyl_pk_request;
+
+/* Spectra of `count` requests issued back to back on the context stream and
+ * waited for once (no reference counterpart: the batched form of
+ * pyl_pk_particles).  The sequence is captured into a CUDA graph the first
+ * time a given list of requests (same pointers, sizes and options) is seen
+ * -- that first call issues the requests directly, which also sizes the
+ * workspaces -- and later calls with the same list launch the graph: one
+ * launch for the whole batch.  outs[i] receives request i (arrays as for
+ * pyl_pk).  All requests use device pointers (PYL_DEVICE_PTRS) or all host
+ * pointers; PYL_NO_GRAPH skips the graph.                                  */
+int pyl_pk_batch(pyl_ctx *ctx, const pyl_pk_request *reqs, int count,
+                 pyl_pk_out *outs, int flags);
 
 /* ---------------------------------------------------------------------
  * Rows around the spectrum (same FFT, window and mode conventions).

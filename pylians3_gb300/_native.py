@@ -33,6 +33,7 @@ PYL_DEPOSIT_SORTED = 0x08
 PYL_SORT_TWO_PASS = 0x10
 PYL_SORT_FRONTIER = 0x20
 PYL_DEPOSIT_FLOAT = 0x40
+PYL_NO_GRAPH = 0x80
 PYL_PK_1D, PYL_PK_2D, PYL_PK_PHASE, PYL_PK_ALL = 0x01, 0x02, 0x04, 0x07
 
 # every symbol include/pylgpu.h declares (checked by the tests)
@@ -44,7 +45,7 @@ EXPORTS = (
     "pyl_ctx_set_timing", "pyl_ctx_stage_times", "pyl_stage_name", "pyl_pk_noalloc",
     "pyl_pk_particles_enqueue", "pyl_pk_query", "pyl_pk_collect",
     "pyl_correct_mas", "pyl_fft2_r2c", "pyl_fft2_c2r", "pyl_pk_plane", "pyl_cic_interp",
-    "pyl_xpk", "pyl_rsd",
+    "pyl_xpk", "pyl_rsd", "pyl_pk_batch",
 )
 
 
@@ -58,6 +59,12 @@ class PkOut(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in (
         "k3D", "Pk", "Nmodes3D", "k1D", "Pk1D", "Nmodes1D", "kpar", "kper",
         "Pk2D", "Nmodes2D", "Pkphase")]
+
+
+class PkRequest(ctypes.Structure):
+    _fields_ = [("pos", ctypes.c_void_p), ("n", ctypes.c_int64), ("W", ctypes.c_void_p),
+                ("dims", ctypes.c_int), ("BoxSize", ctypes.c_float), ("mas_deposit", ctypes.c_int),
+                ("axis", ctypes.c_int), ("mas_window", ctypes.c_int), ("what", ctypes.c_int)]
 
 
 class XPkOut(ctypes.Structure):
@@ -119,6 +126,7 @@ def load():
             "pyl_cic_interp": [vp, vp, i32, f32, vp, i64, vp, i32],
             "pyl_xpk": [vp, vp, i32, i32, f64, i32, vp, ctypes.POINTER(XPkOut), i32],
             "pyl_rsd": [vp, vp, vp, i64, f32, f32, f32, i32, i32],
+            "pyl_pk_batch": [vp, ctypes.POINTER(PkRequest), i32, ctypes.POINTER(PkOut), i32],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)

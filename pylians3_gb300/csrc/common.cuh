@@ -104,6 +104,15 @@ struct pyl_ctx {
     // Status word the kernels set when a bounded wait gives up (bits of
     // kStatusWaitTimeout, async_copy.cuh); read and cleared by status_check.
     unsigned *d_status = nullptr;
+
+    // pyl_pk_batch: while a sequence is captured no workspace may grow (a
+    // reallocation synchronises the stream); the last captured batch, its
+    // key (the request list and flags) and the pinned buffer it writes.
+    bool capturing = false;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<char> batch_key;
+    void *batch_pinned = nullptr;
+    size_t batch_pinned_bytes = 0;
 };
 
 namespace pyl {
@@ -224,6 +233,13 @@ int finalize(pyl_ctx *ctx, const ModeTables &T, const std::vector<double> &raw,
              pyl_pk_out *out);
 int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double> &raw,
                  float2 *dc, double *mass);
+// The particles -> spectrum request (ctx.cu): argument check, issue on the
+// context stream with the result copied to host `dst`, finalisation.
+int check_particles(pyl_ctx *ctx, const pyl_pk_request &r);
+int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, int flags,
+                    void *dst);
+int finalize_particles(pyl_ctx *ctx, const ModeTables &T, const AccLayout &L, const void *src,
+                       int dims, double BoxSize, int what, pyl_pk_out *out);
 void twiddles_host(int n, std::vector<float2> &tw);
 void window_host(int dims, int mas, std::vector<float> &w);
 // Mode tables: sizes of the count arrays, and the tables from the counts.

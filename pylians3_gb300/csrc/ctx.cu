@@ -44,6 +44,11 @@ int status_check(pyl_ctx *ctx) {
 void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status) {
     pyl_ctx::Buf &b = ctx->ws[name];
     if (b.bytes >= bytes && b.p) return b.p;
+    if (ctx->capturing) {
+        *status = fail(ctx, PYL_ERR_STATE, std::string("workspace ") + name +
+                                               " would grow during graph capture");
+        return nullptr;
+    }
     const size_t old = b.p ? b.bytes : 0;
     if (b.p) {
         // the stream may still use the old buffer
@@ -315,6 +320,8 @@ int pyl_ctx_destroy(pyl_ctx *ctx) {
         if (p.b) cudaEventDestroy(p.b);
     }
     if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+    if (ctx->batch_pinned) cudaFreeHost(ctx->batch_pinned);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PYL_OK;
@@ -683,6 +690,77 @@ int finalize(pyl_ctx *ctx, const ModeTables &T, const std::vector<double> &raw,
     return PYL_OK;
 }
 
+int check_particles(pyl_ctx *ctx, const pyl_pk_request &r) {
+    if (r.dims < 2 || r.n <= 0 || !r.pos) return fail(ctx, PYL_ERR_ARG, "bad arguments");
+    if (r.mas_deposit < PYL_MAS_NGP || r.mas_deposit > PYL_MAS_PCS)
+        return fail(ctx, PYL_ERR_ARG, "option not valid!!!");
+    return PYL_OK;
+}
+
+// Issues one particles -> spectrum request on the context stream: upload
+// (host inputs), zero, deposit, the FFT passes and the fused binning, then
+// the raw sums, the k = 0 mode and the mass copied to `dst` (host, pinned).
+int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, int flags,
+                    void *dst) {
+    int st = PYL_OK;
+    const int64_t n = r.n;
+    const int dims = r.dims;
+    const float *dpos = r.pos, *dW = r.W;
+    if (!(flags & PYL_DEVICE_PTRS)) {
+        StageScope s(ctx, ST_H2D);
+        float *p = (float *)ws_get(ctx, "ma_pos", sizeof(float) * (size_t)(3 * n), &st);
+        if (!p) return st;
+        PYL_CUDA(ctx, cudaMemcpyAsync(p, r.pos, sizeof(float) * (size_t)(3 * n),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        dpos = p;
+        if (r.W) {
+            float *w = (float *)ws_get(ctx, "ma_w", sizeof(float) * (size_t)n, &st);
+            if (!w) return st;
+            PYL_CUDA(ctx, cudaMemcpyAsync(w, r.W, sizeof(float) * (size_t)n,
+                                          cudaMemcpyHostToDevice, ctx->stream));
+            dW = w;
+        }
+    }
+    const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
+    float *grid = (float *)ws_get(ctx, "pk_grid", rb, &st);
+    if (!grid) return st;
+    {
+        StageScope s(ctx, ST_ZERO);
+        PYL_CUDA(ctx, cudaMemsetAsync(grid, 0, rb, ctx->stream));
+    }
+    if ((st = deposit(ctx, dpos, n, 3, dW, grid, dims, r.BoxSize, r.mas_deposit, flags)))
+        return st;
+    void *acc = nullptr;
+    AccLayout L;
+    const MassInfo mi{dW, n};
+    if ((st = pk_device(ctx, grid, dims, r.axis, r.mas_window, r.what, T, &acc, L, &mi)))
+        return st;
+    const size_t nb = L.sums() + sizeof(float2) + sizeof(double);
+    StageScope s(ctx, ST_D2H);
+    PYL_CUDA(ctx, cudaMemcpyAsync(dst, acc, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    return PYL_OK;
+}
+
+// Spectrum of a request from the raw sums, k = 0 mode and mass at `src`.
+// The FFT saw rho - shift (shift = mass per cell rounded to float, as on the
+// device); the grid mean is shift + DC / dims^3, and P(delta = rho/mean - 1)
+// = P(rho) / mean^2 for every k != 0.
+int finalize_particles(pyl_ctx *ctx, const ModeTables &T, const AccLayout &L, const void *src,
+                       int dims, double BoxSize, int what, pyl_pk_out *out) {
+    std::vector<double> raw(L.n3 + L.n1 + L.nph + L.n2 + 8);
+    memcpy(raw.data(), src, L.sums());
+    float2 dc;
+    double mass;
+    memcpy(&dc, (const char *)src + L.sums(), sizeof(float2));
+    memcpy(&mass, (const char *)src + L.sums() + sizeof(float2), sizeof(double));
+    const double cells = (double)dims * dims * dims;
+    const double shift = (double)(float)(mass * (1.0 / cells));
+    const double mean = shift + (double)dc.x / cells;
+    if (!(mean > 0.0) && !(mean < 0.0))
+        return fail(ctx, PYL_ERR_ARG, "grid mean is zero: cannot form the overdensity");
+    return finalize(ctx, T, raw, L, BoxSize, what, 1.0 / (mean * mean), true, out);
+}
+
 // Sums, the raw k = 0 mode and the deposited mass back to the host.
 int download_raw(pyl_ctx *ctx, void *acc, const AccLayout &L, std::vector<double> &raw,
                  float2 *dc, double *mass) {
@@ -745,44 +823,15 @@ int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const fl
                              int dims, float BoxSize, int mas_deposit, int axis, int mas_window,
                              int what, int flags) {
     if (!ctx) return PYL_ERR_ARG;
-    if (dims < 2 || n <= 0 || !pos) return fail(ctx, PYL_ERR_ARG, "bad arguments");
-    if (mas_deposit < PYL_MAS_NGP || mas_deposit > PYL_MAS_PCS)
-        return fail(ctx, PYL_ERR_ARG, "option not valid!!!");
     if (ctx->req.active)
         return fail(ctx, PYL_ERR_STATE, "a request is already in flight on this context");
+    pyl_pk_request r{pos, n, W, dims, BoxSize, mas_deposit, axis, mas_window, what};
+    int st = check_particles(ctx, r);
+    if (st) return st;
     PYL_CUDA(ctx, cudaSetDevice(ctx->device));
-    int st = PYL_OK;
     const ModeTables *T = mode_tables(ctx, dims, axis, &st);
     if (!T) return st;
-    const float *dpos = pos, *dW = W;
-    if (!(flags & PYL_DEVICE_PTRS)) {
-        StageScope s(ctx, ST_H2D);
-        float *p = (float *)ws_get(ctx, "ma_pos", sizeof(float) * (size_t)(3 * n), &st);
-        if (!p) return st;
-        PYL_CUDA(ctx, cudaMemcpyAsync(p, pos, sizeof(float) * (size_t)(3 * n),
-                                      cudaMemcpyHostToDevice, ctx->stream));
-        dpos = p;
-        if (W) {
-            float *w = (float *)ws_get(ctx, "ma_w", sizeof(float) * (size_t)n, &st);
-            if (!w) return st;
-            PYL_CUDA(ctx, cudaMemcpyAsync(w, W, sizeof(float) * (size_t)n,
-                                          cudaMemcpyHostToDevice, ctx->stream));
-            dW = w;
-        }
-    }
-    const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
-    float *grid = (float *)ws_get(ctx, "pk_grid", rb, &st);
-    if (!grid) return st;
-    {
-        StageScope s(ctx, ST_ZERO);
-        PYL_CUDA(ctx, cudaMemsetAsync(grid, 0, rb, ctx->stream));
-    }
-    if ((st = deposit(ctx, dpos, n, 3, dW, grid, dims, BoxSize, mas_deposit, flags))) return st;
-    void *acc = nullptr;
-    AccLayout L;
-    const MassInfo mi{dW, n};
-    if ((st = pk_device(ctx, grid, dims, axis, mas_window, what, *T, &acc, L, &mi))) return st;
-    // raw sums, k = 0 mode and mass -> pinned host memory, then the event
+    const AccLayout L = acc_layout(*T);
     const size_t nb = L.sums() + sizeof(float2) + sizeof(double);
     if (ctx->pinned_bytes < nb) {
         if (ctx->pinned) {
@@ -795,10 +844,7 @@ int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const fl
         ctx->pinned_bytes = nb;
     }
     if (!ctx->done) PYL_CUDA(ctx, cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming));
-    {
-        StageScope s(ctx, ST_D2H);
-        PYL_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, acc, nb, cudaMemcpyDeviceToHost, ctx->stream));
-    }
+    if ((st = issue_particles(ctx, r, *T, flags, ctx->pinned))) return st;
     PYL_CUDA(ctx, cudaEventRecord(ctx->done, ctx->stream));
     ctx->req.active = true;
     ctx->req.dims = dims;
@@ -852,22 +898,7 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms) {
     ctx->req.active = false;
     if ((st = status_check(ctx))) return st;
     const pyl_ctx::Request &R = ctx->req;
-    const AccLayout &L = R.L;
-    std::vector<double> raw(L.n3 + L.n1 + L.nph + L.n2 + 8);
-    memcpy(raw.data(), ctx->pinned, L.sums());
-    float2 dc;
-    double mass;
-    memcpy(&dc, (const char *)ctx->pinned + L.sums(), sizeof(float2));
-    memcpy(&mass, (const char *)ctx->pinned + L.sums() + sizeof(float2), sizeof(double));
-    // The FFT saw rho - shift (shift = mass per cell rounded to float, as on
-    // the device); the grid mean is shift + DC / dims^3, and
-    // P(delta = rho/mean - 1) = P(rho) / mean^2 for every k != 0.
-    const double cells = (double)R.dims * R.dims * R.dims;
-    const double shift = (double)(float)(mass * (1.0 / cells));
-    const double mean = shift + (double)dc.x / cells;
-    if (!(mean > 0.0) && !(mean < 0.0))
-        return fail(ctx, PYL_ERR_ARG, "grid mean is zero: cannot form the overdensity");
-    return finalize(ctx, *R.T, raw, L, R.BoxSize, R.what, 1.0 / (mean * mean), true, out);
+    return finalize_particles(ctx, *R.T, R.L, ctx->pinned, R.dims, R.BoxSize, R.what, out);
 }
 
 }  // extern "C"

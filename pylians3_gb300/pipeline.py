@@ -143,3 +143,52 @@ def power_spectra(pos_sets, dims, BoxSize, MAS="CIC", axis=2, W_sets=None, windo
     while inflight:
         finish()
     return results
+
+
+def spectra_batch(requests, ctx=None, graph=True):
+    """Spectra of a list of requests issued back to back and waited for once
+    (pyl_pk_batch): the first call with a given list captures the launch
+    sequence into a CUDA graph, later calls with the same list (same arrays,
+    sizes and options) launch it as one graph.  requests: dicts with the
+    arguments of ``power_spectrum`` (pos, dims, BoxSize, MAS, axis, W,
+    window, what); the positions are all CUDA tensors or all pinned host
+    arrays.  Returns the spectra in order."""
+    reqs = (_native.PkRequest * len(requests))()
+    outs = [_Outputs(int(r["dims"]), int(r.get("what", 0))) for r in requests]
+    outa = (_native.PkOut * len(requests))(*[o.struct for o in outs])
+    keep = []
+    dev = None
+    for i, r in enumerate(requests):
+        pos, W, MAS = r["pos"], r.get("W"), r.get("MAS", "CIC")
+        require_dtype(pos, "float32", "pos")
+        if MAS not in _native.MAS_CODE:
+            raise ValueError("option not valid!!! (MAS must be NGP, CIC, TSC or PCS)")
+        cuda = is_cuda_tensor(pos)
+        if dev is None:
+            dev = cuda
+        elif dev != cuda:
+            raise ValueError("positions must be all CUDA tensors or all host arrays")
+        if cuda:
+            p = pos.contiguous()
+            w = None if W is None else W.contiguous()
+            torch_sync(p)
+            pp, wp = p.data_ptr(), (w.data_ptr() if w is not None else None)
+        else:
+            p = np.ascontiguousarray(pos)
+            w = None if W is None else np.ascontiguousarray(W, np.float32)
+            pp, wp = p.ctypes.data, (w.ctypes.data if w is not None else None)
+        keep.append((p, w))
+        win = MAS_function(MAS if r.get("window") is None else r["window"])
+        reqs[i] = _native.PkRequest(pp, int(pos.shape[0]), wp, int(r["dims"]),
+                                    float(r["BoxSize"]), _native.MAS_CODE[MAS],
+                                    int(r.get("axis", 2)), win, int(r.get("what", 0)))
+    if ctx is None:
+        ctx = _native.context(requests[0]["pos"].device.index or 0 if dev else 0)
+    flags = (_native.PYL_DEVICE_PTRS if dev else 0) | (0 if graph else _native.PYL_NO_GRAPH)
+    _raise_or_exit(ctx, ctx.lib.pyl_pk_batch(ctx.ptr, reqs, len(requests), outa, flags))
+    res = []
+    for o in outs:
+        s = Spectrum()
+        o.assign(s)
+        res.append(s)
+    return res

@@ -129,3 +129,32 @@ def test_power_spectra_matches_single_calls(env):
             assert np.array_equal(one.Nmodes3D, m.Nmodes3D)
             err = np.abs(m.Pk - one.Pk).max(axis=1) / np.abs(one.Pk[:, 0])
             assert err[:dims // 2 + 1].max() <= TOL_PK
+
+
+def test_spectra_batch_graph_equals_single_calls(env):
+    """pyl_pk_batch: the direct first call, the graph relaunch and the
+    one-at-a-time calls give the same spectra (mixed sizes, weights, MAS)."""
+    torch, native, P = env
+    from pylians3_gb300.pipeline import spectra_batch
+    rng = np.random.default_rng(11)
+    reqs = []
+    for i in range(6):
+        dims = int(rng.choice([64, 96, 128]))
+        n = int(dims ** 3 * rng.integers(1, 3))
+        W = None
+        if i % 2:
+            g = torch.Generator(device="cuda").manual_seed(900 + i)
+            W = torch.exp(0.5 * torch.randn(n, generator=g, device="cuda"))
+        reqs.append(dict(pos=make_pos(torch, n, 700 + i), dims=dims, BoxSize=BOX, W=W,
+                         MAS=str(rng.choice(["CIC", "TSC", "PCS"])), axis=int(rng.integers(0, 3))))
+    ctx = native.Context(0)
+    first = spectra_batch(reqs, ctx=ctx)             # issued directly, then captured
+    again = spectra_batch(reqs, ctx=ctx)             # one graph launch
+    direct = spectra_batch(reqs, ctx=ctx, graph=False)
+    for r, a, b, c in zip(reqs, first, again, direct):
+        one = P.power_spectrum(**r)
+        for x in (a, b, c):
+            assert np.array_equal(x.Nmodes3D, one.Nmodes3D)
+            err = np.abs(x.Pk - one.Pk).max(axis=1) / np.abs(one.Pk[:, 0])
+            assert err[:r["dims"] // 2 + 1].max() <= TOL_PK
+    ctx.close()
