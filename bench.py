@@ -455,6 +455,19 @@ def run_batched(a):
     import pylians3_gb300 as P
     from pylians3_gb300.serving import run_batch
     reqs = batched_requests(torch)
+    # autotune the deposit's tile shape and sort granularity per (dims, MAS)
+    # at the median particle count of the batch's requests of that kind
+    import numpy as np
+    from pylians3_gb300 import autotune
+    tuned = {}
+    groups = {}
+    for r in reqs:
+        groups.setdefault((r["dims"], r["MAS"]), []).append(int(r["pos"].shape[0]))
+    for (dims, mas), ns in sorted(groups.items()):
+        default = autotune.current_shape(dims, mas)
+        shape, times = autotune.tune(dims, mas, int(np.median(ns)), use_cache=False)
+        tuned["%d/%s" % (dims, mas)] = {"shape": list(shape), "default": list(default),
+                                        "ms": times.get(shape), "default_ms": times.get(default)}
     for r in reqs[:4]:
         P.power_spectrum(**r)          # plans, mode tables
     ctx = P.context(0)
@@ -482,6 +495,7 @@ def run_batched(a):
             "api": "pipeline.spectra_batch: the 64 requests as one CUDA graph launch",
             "sequential_value": len(reqs) / t_seq, "speedup": t_seq / t_graph,
             "server_value": len(reqs) / t_srv, "server_slots": slots,
+            "autotune": tuned,
             "particles_total": int(sum(r["pos"].shape[0] for r in reqs)),
             "config": {"dims": "U{128,192,256,384}", "particles": "2^U(20,25)",
                        "positions": "uniform | zeldovich sigma U(2,5)", "W": "lognormal(0,0.5) half",

@@ -211,6 +211,17 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms);
 int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double BoxSize,
                    int axis, int mas, int what, pyl_pk_out *out);
 
+/* Tile shape of the sorted deposit for (dims, mas): tiles of TX x TY x TZ
+ * cells (powers of two, at most 64) and F tiles per coarse bucket of the
+ * first partition pass (a power of two <= 256; 0 = about sqrt(tiles)).  No
+ * reference counterpart: set by the autotuner (pylians3_gb300.autotune) for
+ * the whole process; TX = 0 restores the built-in rule.  Returns
+ * PYL_ERR_UNSUPPORTED for shapes whose footprint or tile histogram does not
+ * fit in shared memory or that need more than 256 coarse buckets.
+ * pyl_get_tile_shape reports the shape in use.                             */
+int pyl_set_tile_shape(int dims, int mas, int TX, int TY, int TZ, int F);
+int pyl_get_tile_shape(int dims, int mas, int *TX, int *TY, int *TZ, int *F);
+
 /* One particles -> spectrum request (the arguments of pyl_pk_particles). */
 typedef struct {
     const float *pos;   /* (n, 3) positions                                */

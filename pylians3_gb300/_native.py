@@ -45,7 +45,7 @@ EXPORTS = (
     "pyl_ctx_set_timing", "pyl_ctx_stage_times", "pyl_stage_name", "pyl_pk_noalloc",
     "pyl_pk_particles_enqueue", "pyl_pk_query", "pyl_pk_collect",
     "pyl_correct_mas", "pyl_fft2_r2c", "pyl_fft2_c2r", "pyl_pk_plane", "pyl_cic_interp",
-    "pyl_xpk", "pyl_rsd", "pyl_pk_batch",
+    "pyl_xpk", "pyl_rsd", "pyl_pk_batch", "pyl_set_tile_shape", "pyl_get_tile_shape",
 )
 
 
@@ -127,6 +127,8 @@ def load():
             "pyl_xpk": [vp, vp, i32, i32, f64, i32, vp, ctypes.POINTER(XPkOut), i32],
             "pyl_rsd": [vp, vp, vp, i64, f32, f32, f32, i32, i32],
             "pyl_pk_batch": [vp, ctypes.POINTER(PkRequest), i32, ctypes.POINTER(PkOut), i32],
+            "pyl_set_tile_shape": [i32, i32, i32, i32, i32, i32],
+            "pyl_get_tile_shape": [i32, i32] + [ctypes.POINTER(i32)] * 4,
         }
         for name, args in sig.items():
             fn = getattr(lib, name)

@@ -23,6 +23,7 @@
 // index 0 and weight 1 for every tap, so a particle is deposited 2/3/4 times
 // onto the same plane for CIC/TSC/PCS (and renormalised by the caller).
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 
 #include "async_copy.cuh"
@@ -897,7 +898,63 @@ int set_smem(pyl_ctx *ctx, K kernel, size_t bytes) {
     return PYL_OK;
 }
 
+// Tile shapes chosen by the autotuner (pyl_set_tile_shape), per (dims, MAS);
+// make_geom's rule applies where none is set.
+struct TileShape {
+    int TX, TY, TZ, F;
+};
+std::mutex g_shape_mu;
+std::map<std::pair<int, int>, TileShape> g_shape;
+
+int ilog2_ceil(int v) {
+    int s = 0;
+    while ((1 << s) < v) ++s;
+    return s;
+}
+
+// Fills the derived fields of a geometry with tile extents TX, TY, TZ and F
+// tiles per coarse bucket (F = 0: ~sqrt(ntiles)).
+void finish_geom(TileGeom &g, int dims, int mas, int F) {
+    g.dims = dims;
+    g.ntx = (dims + g.TX - 1) / g.TX;
+    g.nty = (dims + g.TY - 1) / g.TY;
+    g.ntz = (dims + g.TZ - 1) / g.TZ;
+    g.ntiles = g.ntx * g.nty * g.ntz;
+    g.sx = ilog2_ceil(g.TX);
+    g.sy = ilog2_ceil(g.TY);
+    g.sz = ilog2_ceil(g.TZ);
+    const int lo = (mas == PYL_MAS_TSC || mas == PYL_MAS_PCS) ? 1 : 0;
+    const int hi = (mas == PYL_MAS_TSC || mas == PYL_MAS_PCS) ? 2 : 1;
+    g.RX = g.TX + lo + hi;
+    g.RY = g.TY + lo + hi;
+    g.RZ = g.TZ + lo + hi;
+    if (F > 0) {
+        g.F = F;
+    } else {
+        // coarse buckets: ~sqrt(ntiles) tiles each, at most kMaxKeys buckets
+        g.F = 1;
+        while ((long long)g.F * g.F < g.ntiles) g.F *= 2;
+        while ((g.ntiles + g.F - 1) / g.F > kMaxKeys) g.F *= 2;
+        if (g.F > kMaxKeys) g.F = kMaxKeys;
+    }
+    g.ncoarse = (g.ntiles + g.F - 1) / g.F;
+}
+
+bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
 TileGeom make_geom(int dims, int mas) {
+    {
+        std::lock_guard<std::mutex> lock(g_shape_mu);
+        auto it = g_shape.find(std::make_pair(dims, mas));
+        if (it != g_shape.end()) {
+            TileGeom g;
+            g.TX = it->second.TX;
+            g.TY = it->second.TY;
+            g.TZ = it->second.TZ;
+            finish_geom(g, dims, mas, it->second.F);
+            return g;
+        }
+    }
     TileGeom g;
     g.dims = dims;
     int p2 = 1;   // largest power of two <= dims, at most 32
@@ -1205,3 +1262,44 @@ int scale_grid_f64(pyl_ctx *ctx, double *grid, int64_t count, double s) {
 }
 
 }  // namespace pyl
+
+using pyl::TileGeom;
+
+extern "C" {
+
+int pyl_set_tile_shape(int dims, int mas, int TX, int TY, int TZ, int F) {
+    if (dims < 2 || mas < PYL_MAS_NGP || mas > PYL_MAS_PCS) return PYL_ERR_ARG;
+    const auto key = std::make_pair(dims, mas);
+    std::lock_guard<std::mutex> lock(pyl::g_shape_mu);
+    if (TX == 0) {
+        pyl::g_shape.erase(key);
+        return PYL_OK;
+    }
+    if (!pyl::pow2(TX) || !pyl::pow2(TY) || !pyl::pow2(TZ) || TX > 64 || TY > 64 || TZ > 64 ||
+        (F != 0 && (!pyl::pow2(F) || F > pyl::kMaxKeys)))
+        return PYL_ERR_ARG;
+    TileGeom g;
+    g.TX = TX;
+    g.TY = TY;
+    g.TZ = TZ;
+    pyl::finish_geom(g, dims, mas, F);
+    // the sorted deposit's limits: footprint and tile histogram in shared
+    // memory, at most kMaxKeys keys per partition pass
+    if (sizeof(float) * (size_t)g.RX * g.RY * g.RZ > 200 * 1024 ||
+        (size_t)g.ntiles * 4 > 200 * 1024 || g.ncoarse > pyl::kMaxKeys || g.F > pyl::kMaxKeys)
+        return PYL_ERR_UNSUPPORTED;
+    pyl::g_shape[key] = pyl::TileShape{TX, TY, TZ, g.F};
+    return PYL_OK;
+}
+
+int pyl_get_tile_shape(int dims, int mas, int *TX, int *TY, int *TZ, int *F) {
+    if (dims < 2 || !TX || !TY || !TZ || !F) return PYL_ERR_ARG;
+    const TileGeom g = pyl::make_geom(dims, mas);
+    *TX = g.TX;
+    *TY = g.TY;
+    *TZ = g.TZ;
+    *F = g.F;
+    return PYL_OK;
+}
+
+}  // extern "C"

@@ -99,3 +99,22 @@ def test_product_never_imports_the_oracle():
                 src = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in src and "from oracle" not in src, f
                 assert "liborc" not in src, f
+
+
+def test_tile_shape_validation():
+    """pyl_set_tile_shape checks shapes on the host (no GPU needed)."""
+    import ctypes
+    from pylians3_gb300 import _native as N
+    lib = N.load()
+    v = [ctypes.c_int() for _ in range(4)]
+    assert lib.pyl_get_tile_shape(512, 2, *[ctypes.byref(x) for x in v]) == N.PYL_OK
+    default = [x.value for x in v]
+    assert lib.pyl_set_tile_shape(512, 2, 12, 32, 32, 0) == N.PYL_ERR_ARG       # not 2^k
+    assert lib.pyl_set_tile_shape(512, 4, 64, 64, 64, 0) == N.PYL_ERR_UNSUPPORTED  # footprint
+    assert lib.pyl_set_tile_shape(512, 2, 8, 8, 16, 0) == N.PYL_ERR_UNSUPPORTED   # > 256 buckets
+    assert lib.pyl_set_tile_shape(512, 2, 32, 32, 32, 16) == N.PYL_OK
+    lib.pyl_get_tile_shape(512, 2, *[ctypes.byref(x) for x in v])
+    assert [x.value for x in v] == [32, 32, 32, 16]
+    assert lib.pyl_set_tile_shape(512, 2, 0, 0, 0, 0) == N.PYL_OK
+    lib.pyl_get_tile_shape(512, 2, *[ctypes.byref(x) for x in v])
+    assert [x.value for x in v] == default
