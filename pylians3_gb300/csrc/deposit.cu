@@ -645,7 +645,8 @@ __device__ __forceinline__ T box_line(T *a, int n, int st, bool write) {
         const int j = k - LO;
         if (j >= 0) {
             if (write) a[j * st] = sum;
-            best = best > sum ? best : sum;
+            // the largest window; a NaN (a NaN weight) sticks
+            if (best == best && (sum > best || sum != sum)) best = sum;
         }
     }
     return best;
@@ -699,6 +700,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         __syncthreads();
         float scale = 1.f, inv_scale = 1.f;
         bool fixed = FIXED;   // this item in fixed point
+        bool exact_mass = false;   // ... with per-particle mass-exact rounding
         if (FIXED) {
             // ---- home-cell occupancy (or |W| per home cell), its box sums,
             // their maximum, the scale
@@ -755,15 +757,16 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 m = (s_max[w] > m || s_max[w] != s_max[w]) ? s_max[w] : m;
             // 2^e <= 2^30 / (WMAX * largest box sum); float box sums of |W|
             // get a margin for their rounding
-            const float bound =
-                fmaxf(TapBound<MAS>::WMAX * m * (HAS_W ? 1.001f : 1.f), 1.f);
-            fixed = bound < 1.0e30f;               // false for inf and NaN
+            const float raw = TapBound<MAS>::WMAX * m * (HAS_W ? 1.001f : 1.f);
+            fixed = raw < 1.0e30f;                 // false for inf and NaN weights
             if (fixed) {
+                const float bound = fmaxf(raw, 1.f);
                 int e;
                 frexpf(bound, &e);                 // bound < 2^e
                 e = min(30 - e, 30);
                 scale = ldexpf(1.f, e);
                 inv_scale = ldexpf(1.f, -e);
+                exact_mass = e < 20;
             }
             __syncthreads();   // s_max is rewritten by the next item
         }
@@ -797,6 +800,66 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
 #pragma unroll
                 for (int j = 0; j < NT; ++j) lz[j] = base + o[j];
             }
+            if (FIXED && fixed) {
+                // Each tap rounded to the item's fixed point.  In items whose
+                // scale is coarse (dense clumps, 2^e < 2^20), the particle's
+                // rounding residue -- its quantized mass minus the sum of its
+                // quantized taps -- also goes to its largest tap, so that the
+                // many tiny outer taps rounding to zero cannot bias the mass.
+                if (!exact_mass) {
+#pragma unroll
+                    for (int l = 0; l < NT; ++l)
+#pragma unroll
+                        for (int m = 0; m < NT; ++m) {
+                            const float wxy = wx[l] * wy[m];
+                            const int row = (lx[l] * RY + ly[m]) * RZ;
+#pragma unroll
+                            for (int q = 0; q < NT; ++q) {
+                                float v = wxy * wz[q];
+                                if (HAS_W) v *= wt;
+                                atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
+                            }
+                        }
+                    return;
+                }
+                int sum = 0;
+#pragma unroll
+                for (int l = 0; l < NT; ++l)
+#pragma unroll
+                    for (int m = 0; m < NT; ++m) {
+                        const float wxy = wx[l] * wy[m];
+#pragma unroll
+                        for (int q = 0; q < NT; ++q) {
+                            float v = wxy * wz[q];
+                            if (HAS_W) v *= wt;
+                            sum += __float2int_rn(v * scale);
+                        }
+                    }
+                int al = 0, am = 0, aq = 0;
+#pragma unroll
+                for (int j = 1; j < NT; ++j) {
+                    if (wx[j] > wx[al]) al = j;
+                    if (wy[j] > wy[am]) am = j;
+                    if (wz[j] > wz[aq]) aq = j;
+                }
+                const int residue = (HAS_W ? __float2int_rn(wt * scale) : (int)scale) - sum;
+#pragma unroll
+                for (int l = 0; l < NT; ++l)
+#pragma unroll
+                    for (int m = 0; m < NT; ++m) {
+                        const float wxy = wx[l] * wy[m];
+                        const int row = (lx[l] * RY + ly[m]) * RZ;
+#pragma unroll
+                        for (int q = 0; q < NT; ++q) {
+                            float v = wxy * wz[q];
+                            if (HAS_W) v *= wt;
+                            int iv = __float2int_rn(v * scale);
+                            if (l == al && m == am && q == aq) iv += residue;
+                            atomicAdd(s_int + row + lz[q], iv);
+                        }
+                    }
+                return;
+            }
 #pragma unroll
             for (int l = 0; l < NT; ++l) {
 #pragma unroll
@@ -807,9 +870,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                     for (int q = 0; q < NT; ++q) {
                         float v = wxy * wz[q];
                         if (HAS_W) v *= wt;
-                        if (FIXED && fixed)
-                            atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
-                        else if (COMP) comp_add(s_reg + row + lz[q], s_reg + cells + row + lz[q], v);
+                        if (COMP) comp_add(s_reg + row + lz[q], s_reg + cells + row + lz[q], v);
                         else atomicAdd(s_reg + row + lz[q], v);
                     }
                 }
