@@ -354,6 +354,90 @@ k_tile_count(const float *__restrict__ pos, long long n, float inv, TileGeom g,
     if (threadIdx.x == 0 && s_distinct) atomicAdd(distinct, s_distinct);
 }
 
+// The same count with 16-byte loads (positions 16-byte aligned): a thread
+// takes four consecutive particles as three float4 (a warp reads 1536
+// contiguous bytes per load instruction), two groups in flight; runs of one
+// tile inside a thread take one shared atomic, a warp whose 128 particles
+// share a tile takes one.  Tile changes are counted between consecutive
+// particles (inside a thread and across neighbouring lanes), plus one per
+// warp group.  The last n % 4 particles are counted by block 0 one by one.
+template <int MAS>
+__global__ void __launch_bounds__(1024, 1)
+k_tile_count4(const float4 *__restrict__ pos4, const float *__restrict__ pos, long long n,
+              float inv, TileGeom g, unsigned *__restrict__ count,
+              unsigned *__restrict__ distinct) {
+    extern __shared__ unsigned s_cnt[];
+    __shared__ unsigned s_distinct;
+    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x) s_cnt[t] = 0u;
+    if (threadIdx.x == 0) s_distinct = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    unsigned changes = 0;
+    const long long groups = n / 4;          // groups of four particles
+    constexpr int U = 2;
+    const long long step = (long long)gridDim.x * blockDim.x * U;
+    for (long long b = (long long)blockIdx.x * blockDim.x * U; b < groups; b += step) {
+        float4 a[U][3];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long gi = b + (long long)u * blockDim.x + threadIdx.x;
+            if (gi < groups) {
+                a[u][0] = __ldcs(pos4 + 3 * gi);
+                a[u][1] = __ldcs(pos4 + 3 * gi + 1);
+                a[u][2] = __ldcs(pos4 + 3 * gi + 2);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long gi = b + (long long)u * blockDim.x + threadIdx.x;
+            const bool active = gi < groups;
+            int t[4] = {-1, -1, -1, -1};
+            if (active) {
+                const float4 p0 = a[u][0], p1 = a[u][1], p2 = a[u][2];
+                t[0] = tile_of<MAS>(p0.x, p0.y, p0.z, inv, g);
+                t[1] = tile_of<MAS>(p0.w, p1.x, p1.y, inv, g);
+                t[2] = tile_of<MAS>(p1.z, p1.w, p2.x, inv, g);
+                t[3] = tile_of<MAS>(p2.y, p2.z, p2.w, inv, g);
+            }
+            const int prev_last = __shfl_up_sync(0xffffffffu, t[3], 1);
+            const int first = __shfl_sync(0xffffffffu, t[0], 0);
+            const bool same = __all_sync(0xffffffffu, t[0] == first && t[1] == first &&
+                                                          t[2] == first && t[3] == first);
+            if (same) {
+                if (lane == 0 && first >= 0) {
+                    atomicAdd(&s_cnt[first], 128u);
+                    changes += 1u;
+                }
+            } else if (active) {
+                changes += (lane == 0 || t[0] != prev_last) ? 1u : 0u;
+                unsigned run = 1u;
+#pragma unroll
+                for (int k = 1; k < 4; ++k) {
+                    if (t[k] == t[k - 1]) {
+                        ++run;
+                    } else {
+                        atomicAdd(&s_cnt[t[k - 1]], run);
+                        run = 1u;
+                        ++changes;
+                    }
+                }
+                atomicAdd(&s_cnt[t[3]], run);
+            }
+        }
+    }
+    if (blockIdx.x == 0) {
+        for (long long i = groups * 4 + threadIdx.x; i < n; i += blockDim.x)
+            atomicAdd(&s_cnt[tile_of<MAS>(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], inv, g)], 1u);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) changes += __shfl_down_sync(0xffffffffu, changes, o);
+    if (lane == 0 && changes) atomicAdd(&s_distinct, changes);
+    __syncthreads();
+    for (int t = threadIdx.x; t < g.ntiles; t += blockDim.x)
+        if (s_cnt[t]) atomicAdd(&count[t], s_cnt[t]);
+    if (threadIdx.x == 0 && s_distinct) atomicAdd(distinct, s_distinct);
+}
+
 // After the scan (start[0..ntiles] exclusive, start[ntiles] = n): the key
 // cursors of both passes and the deposit work items (tile, chunk) of every
 // non-empty tile, chunk = kItemCap particles.  nchunk is scanned separately.
@@ -1106,8 +1190,14 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         PYL_CUDA(ctx, cudaMemsetAsync(start, 0, sizeof(unsigned) * (size_t)(nt + 1), ctx->stream));
         PYL_CUDA(ctx, cudaMemsetAsync(flags2, 0, 2 * sizeof(unsigned), ctx->stream));
         const size_t hsm = sizeof(unsigned) * (size_t)nt;
-        if ((st = set_smem(ctx, k_tile_count<MAS>, hsm))) return st;
-        k_tile_count<MAS><<<sms, 1024, hsm, ctx->stream>>>(pos, n, inv, g, start, distinct);
+        if (((uintptr_t)pos & 15) == 0) {
+            if ((st = set_smem(ctx, k_tile_count4<MAS>, hsm))) return st;
+            k_tile_count4<MAS><<<sms, 1024, hsm, ctx->stream>>>(
+                reinterpret_cast<const float4 *>(pos), pos, n, inv, g, start, distinct);
+        } else {
+            if ((st = set_smem(ctx, k_tile_count<MAS>, hsm))) return st;
+            k_tile_count<MAS><<<sms, 1024, hsm, ctx->stream>>>(pos, n, inv, g, start, distinct);
+        }
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         // exclusive scan over nt+1 entries (the extra 0 becomes the total n)
