@@ -742,11 +742,14 @@ __device__ __forceinline__ T box_line(T *a, int n, int st, bool write) {
 // FIXED: the footprint is accumulated in 32-bit integers, each tap rounded
 // to a fixed point of scale 2^e.  A first pass over the item's particles
 // histograms their home cells (counts, or sums of |W| for weighted
-// particles); a box sum of the histogram over the stencil's reach gives, for
-// every footprint cell, how much mass can reach it, so no cell can exceed
-// WMAX times the largest box sum, and 2^e is the largest power of two keeping
-// that bound under 2^30.  An item whose bound is not finite (weights of inf
-// or NaN) falls back to float atomics.
+// particles).  A footprint cell can only be reached from the R^3 home cells
+// around it, so no cell can exceed WMAX * R^3 * (largest home cell); where
+// that leaves at least 21 fractional bits it sets the scale.  Otherwise
+// (dense clumps) a box sum of the histogram over the stencil's reach gives,
+// for every footprint cell, how much mass can reach it, and the largest box
+// sum sets it.  2^e is the largest power of two keeping WMAX times the bound
+// under 2^30.  An item whose bound is not finite (weights of inf or NaN)
+// falls back to float atomics.
 // Integer shared atomics run at about twice the rate of float ones, and the
 // sums are exact (independent of the order of the atomics); the flush
 // converts each cell once (int -> float rounding, then an exact scaling by
@@ -756,6 +759,35 @@ __device__ __forceinline__ T box_line(T *a, int n, int st, bool write) {
 // of TwoSum rounding errors (comp_add), merged into the grid and into the
 // error grid glo with compensated global atomics.
 constexpr int kAccFloat = 0, kAccFixed = 1, kAccComp = 2;
+
+// Largest value over the CTA (a NaN anywhere gives NaN); all threads get it.
+__device__ __forceinline__ float block_max_nan(float m, float *s_max) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float b = __shfl_xor_sync(0xffffffffu, m, o);
+        m = (b > m || b != b) ? b : m;
+    }
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+        m = (s_max[w] > m || s_max[w] != s_max[w]) ? s_max[w] : m;
+    __syncthreads();   // s_max may be written again
+    return m;
+}
+
+// Fixed-point exponent for footprint cells whose mass is at most m: the
+// largest e with WMAX * m * 2^e < 2^30 (at most 30).  Float sums of |W| get
+// a margin for their rounding.  False when m is not finite (inf or NaN
+// weights): the item then accumulates in float.
+template <int MAS, bool HAS_W>
+__device__ __forceinline__ bool fixed_exponent(float m, int &e) {
+    const float raw = TapBound<MAS>::WMAX * m * (HAS_W ? 1.001f : 1.f);
+    if (!(raw < 1.0e30f)) return false;
+    frexpf(fmaxf(raw, 1.f), &e);   // bound < 2^e
+    e = min(30 - e, 30);
+    return true;
+}
 
 template <int MAS, bool HAS_W, int ACC>
 __global__ void __launch_bounds__(512)
@@ -786,15 +818,21 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
         bool fixed = FIXED;   // this item in fixed point
         bool exact_mass = false;   // ... with per-particle mass-exact rounding
         if (FIXED) {
-            // ---- home-cell occupancy (or |W| per home cell), its box sums,
-            // their maximum, the scale
+            // ---- home-cell occupancy (counts, or sums of |W|), the largest
+            // home cell, and from it (or from box sums) the scale
+            int lmi = 0;       // largest count this thread has seen
+            float lmf = 0.f;   // ... or largest sum of |W| (a NaN sticks)
             auto occupy = [&](float x, float y, float z, float w) {
                 const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
                 const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
                 const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
                 const int c = ((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ + (hz - oz + S::LO);
-                if (HAS_W) atomicAdd(&s_reg[c], fabsf(w));
-                else atomicAdd(&s_int[c], 1);
+                if (HAS_W) {
+                    const float o = atomicAdd(&s_reg[c], fabsf(w)) + fabsf(w);
+                    lmf = (o > lmf || o != o) ? o : lmf;
+                } else {
+                    lmi = max(lmi, atomicAdd(&s_int[c], 1) + 1);
+                }
             };
             // two particles per thread and step, both loaded first
             for (long long i = p0 + threadIdx.x; i < p1; i += 2 * blockDim.x) {
@@ -812,47 +850,38 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 occupy(x, y, z, w);
                 if (i2 < p1) occupy(x2, y2, z2, w2);
             }
-            __syncthreads();
-            // separable box sums: z lines, y lines, then x lines (max only)
-            using T = typename std::conditional<HAS_W, float, int>::type;
-            T *hs = reinterpret_cast<T *>(s_reg);
-            for (int l = threadIdx.x; l < RX * RY; l += blockDim.x)
-                box_line<S::LO, S::HI, T>(hs + l * RZ, RZ, 1, true);
-            __syncthreads();
-            for (int l = threadIdx.x; l < RX * RZ; l += blockDim.x)
-                box_line<S::LO, S::HI, T>(hs + (l / RZ) * RY * RZ + (l % RZ), RY, RZ, true);
-            __syncthreads();
-            float m = 0.f;
-            for (int l = threadIdx.x; l < RY * RZ; l += blockDim.x) {
-                const float b = (float)box_line<S::LO, S::HI, T>(hs + l, RX, RY * RZ, false);
-                m = (b > m || b != b) ? b : m;        // keeps a NaN
+            // A footprint cell takes taps from the home cells of an R^3 box
+            // only, so R^3 times the largest home cell bounds every cell.
+            // Where that bound leaves fewer than 21 fractional bits (dense
+            // clumps), the box sums of the histogram give the tight bound.
+            constexpr int R = S::LO + S::HI + 1;
+            int e = 0;
+            fixed = fixed_exponent<MAS, HAS_W>(
+                block_max_nan(HAS_W ? lmf : (float)lmi, s_max) * (float)(R * R * R), e);
+            if (fixed && e < 21) {
+                // separable box sums: z lines, y lines, then x lines (max only)
+                using T = typename std::conditional<HAS_W, float, int>::type;
+                T *hs = reinterpret_cast<T *>(s_reg);
+                for (int l = threadIdx.x; l < RX * RY; l += blockDim.x)
+                    box_line<S::LO, S::HI, T>(hs + l * RZ, RZ, 1, true);
+                __syncthreads();
+                for (int l = threadIdx.x; l < RX * RZ; l += blockDim.x)
+                    box_line<S::LO, S::HI, T>(hs + (l / RZ) * RY * RZ + (l % RZ), RY, RZ, true);
+                __syncthreads();
+                float m = 0.f;
+                for (int l = threadIdx.x; l < RY * RZ; l += blockDim.x) {
+                    const float b = (float)box_line<S::LO, S::HI, T>(hs + l, RX, RY * RZ, false);
+                    m = (b > m || b != b) ? b : m;        // keeps a NaN
+                }
+                fixed = fixed_exponent<MAS, HAS_W>(block_max_nan(m, s_max), e);
             }
-            __syncthreads();
             for (int i = threadIdx.x; i < cells; i += blockDim.x) s_int[i] = 0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float b = __shfl_xor_sync(0xffffffffu, m, o);
-                m = (b > m || b != b) ? b : m;
-            }
-            if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
             __syncthreads();
-            m = 0.f;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-                m = (s_max[w] > m || s_max[w] != s_max[w]) ? s_max[w] : m;
-            // 2^e <= 2^30 / (WMAX * largest box sum); float box sums of |W|
-            // get a margin for their rounding
-            const float raw = TapBound<MAS>::WMAX * m * (HAS_W ? 1.001f : 1.f);
-            fixed = raw < 1.0e30f;                 // false for inf and NaN weights
             if (fixed) {
-                const float bound = fmaxf(raw, 1.f);
-                int e;
-                frexpf(bound, &e);                 // bound < 2^e
-                e = min(30 - e, 30);
                 scale = ldexpf(1.f, e);
                 inv_scale = ldexpf(1.f, -e);
                 exact_mass = e < 20;
             }
-            __syncthreads();   // s_max is rewritten by the next item
         }
         auto deposit_one = [&](float px, float py, float pz, float wt) {
             int lx[NT], ly[NT], lz[NT];
