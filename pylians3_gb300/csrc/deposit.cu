@@ -797,6 +797,14 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                float *__restrict__ grid, int vec4, float *__restrict__ glo) {
     constexpr bool FIXED = ACC == kAccFixed;
     constexpr bool COMP = ACC == kAccComp;
+    // Fewest fractional bits a fixed-point item may keep; an item whose bound
+    // leaves fewer accumulates in float.  PCS: the deconvolution amplifies
+    // the grid's rounding noise ~5e4-fold in the corner bins beyond the
+    // Nyquist wavenumber, so a PCS item takes fixed point only where its
+    // quantization noise (64 taps of at most 2^-25 each per cell) stays
+    // below that of float32 accumulation; tiles holding dense halos keep
+    // float atomics.
+    constexpr int MIN_BITS = MAS == PYL_MAS_PCS ? 24 : 0;
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
     extern __shared__ float s_reg[];
@@ -855,10 +863,11 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             // Where that bound leaves fewer than 21 fractional bits (dense
             // clumps), the box sums of the histogram give the tight bound.
             constexpr int R = S::LO + S::HI + 1;
+            constexpr int FAST_BITS = MIN_BITS > 21 ? MIN_BITS : 21;
             int e = 0;
             fixed = fixed_exponent<MAS, HAS_W>(
                 block_max_nan(HAS_W ? lmf : (float)lmi, s_max) * (float)(R * R * R), e);
-            if (fixed && e < 21) {
+            if (fixed && e < FAST_BITS) {
                 // separable box sums: z lines, y lines, then x lines (max only)
                 using T = typename std::conditional<HAS_W, float, int>::type;
                 T *hs = reinterpret_cast<T *>(s_reg);
@@ -875,12 +884,13 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 }
                 fixed = fixed_exponent<MAS, HAS_W>(block_max_nan(m, s_max), e);
             }
+            if (e < MIN_BITS) fixed = false;   // too coarse: float for this item
             for (int i = threadIdx.x; i < cells; i += blockDim.x) s_int[i] = 0;
             __syncthreads();
             if (fixed) {
                 scale = ldexpf(1.f, e);
                 inv_scale = ldexpf(1.f, -e);
-                exact_mass = e < 20;
+                exact_mass = MIN_BITS < 20 && e < 20;
             }
         }
         auto deposit_one = [&](float px, float py, float pz, float wt) {
@@ -919,7 +929,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 // rounding residue -- its quantized mass minus the sum of its
                 // quantized taps -- also goes to its largest tap, so that the
                 // many tiny outer taps rounding to zero cannot bias the mass.
-                if (!exact_mass) {
+                if (MIN_BITS >= 20 || !exact_mass) {
 #pragma unroll
                     for (int l = 0; l < NT; ++l)
 #pragma unroll
@@ -1306,14 +1316,10 @@ int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, f
     const TileGeom g = make_geom(dims, MAS);
     const int forced = (flags & PYL_SORT_TWO_PASS) ? kSortTwoPass
                        : (flags & PYL_SORT_FRONTIER) ? kSortFrontier : -1;
-    // Compensated if asked for; else NGP/CIC/TSC accumulate in fixed point
-    // unless float atomics are asked for.  PCS keeps float
-    // atomics: its deconvolution amplifies the grid's rounding noise ~5e4-fold
-    // in the corner bins beyond the Nyquist wavenumber, and the coarser
-    // quantization of tiles holding dense halos shows there.
-    const int acc = glo ? kAccComp
-                        : (MAS != PYL_MAS_PCS && !(flags & PYL_DEPOSIT_FLOAT)) ? kAccFixed
-                                                                              : kAccFloat;
+    // Compensated if asked for; else fixed point (PCS: per item, where the
+    // scale keeps at least 24 fractional bits) unless float atomics are
+    // asked for.
+    const int acc = glo ? kAccComp : !(flags & PYL_DEPOSIT_FLOAT) ? kAccFixed : kAccFloat;
     return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo)
              : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo);
 }

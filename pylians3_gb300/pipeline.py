@@ -27,7 +27,7 @@ class Spectrum:
 
 
 DEPOSIT_FLAGS = {
-    "auto": 0,                                   # fixed-point tiles for unit weights
+    "auto": 0,                                   # fixed-point tiles (PCS: where 24 bits fit)
     "float": _native.PYL_DEPOSIT_FLOAT,          # float32 shared atomics
     "compensated": _native.PYL_COMPENSATED,      # float32 + TwoSum error grid
 }
