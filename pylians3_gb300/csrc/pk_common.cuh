@@ -136,9 +136,11 @@ __device__ __forceinline__ void bin_mode_run(BinRun &R, Hist &H, const PkAcc &ac
 // L consecutive modes kxx0 .. kxx0+L-1 of one pencil (ky, kz fixed), read
 // from shared memory at ln[pad(kxx)], the window at win[pad(kxx)] (the pad
 // spreads the L-strided accesses of a warp over the banks): the same work as
-// bin_mode_run, with the
-// bin index updated incrementally (n2 changes by 2 kx + 1 between neighbours)
-// instead of one square root per mode.
+// bin_mode_run, with the bin index updated incrementally instead of one
+// square root per mode.  Between neighbours |kx| changes by one, so
+// sqrt(kx^2 + ky^2 + kz^2) changes by at most one and the bin by -1, 0 or +1.
+// Pencils off the kz = 0 and kz = mid planes (all but two planes) need none
+// of the half-space checks and hold no DC mode: they take a branch-free body.
 template <int WHAT, int L, class Hist, class Pad>
 __device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 *ln, Pad pad,
                                          int kxx0, int ky, int kz, int n, int axis,
@@ -149,24 +151,41 @@ __device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 
     const int kx0 = kxx0 > mid ? kxx0 - n : kxx0;
     int bin = isqrt_dev(kx0 * kx0 + r2);
     BinRun R;
+    if (!plane) {
+        const int kpar_c = axis == 1 ? ky : kz;   // kpar when it is not kx
+#pragma unroll
+        for (int i = 0; i < L; ++i) {
+            const int kxx = kxx0 + i;
+            const int kx = kxx > mid ? kxx - n : kxx;
+            const int n2 = kx * kx + r2;          // > 0: kz != 0 here
+            bin += ((bin + 1) * (bin + 1) <= n2) - (bin * bin > n2);
+            const float2 v = ln[pad(kxx)];
+            const int kpar = axis == 0 ? kx : kpar_c;
+            const float f = win[pad(kxx)] * wyz;
+            const float re = v.x * f, im = v.y * f;
+            const float d2 = re * re + im * im;
+            const float mu2 = __fdividef((float)(kpar * kpar), (float)n2);
+            R.add(H, bin, d2, mu2);
+            if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
+        }
+        R.flush(H);
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < L; ++i) {
         const int kxx = kxx0 + i;
         const int kx = kxx > mid ? kxx - n : kxx;
         const int n2 = kx * kx + r2;
-        while (bin * bin > n2) --bin;
-        while ((bin + 1) * (bin + 1) <= n2) ++bin;
-        if (plane) {
-            if (kx < 0) continue;
-            if ((kx == 0 || (kx == mid && even)) && ky < 0) continue;
-        }
+        bin += ((bin + 1) * (bin + 1) <= n2) - (bin * bin > n2);
+        if (kx < 0) continue;
+        if ((kx == 0 || (kx == mid && even)) && ky < 0) continue;
         const float2 v = ln[pad(kxx)];
         if (n2 == 0) *acc.dc = v;
         const int kpar = axis == 0 ? kx : (axis == 1 ? ky : kz);
         const float f = win[pad(kxx)] * wyz;
         const float re = v.x * f, im = v.y * f;
         const float d2 = re * re + im * im;
-        const float mu2 = n2 > 0 ? (float)(kpar * kpar) * __frcp_rn((float)n2) : 0.f;
+        const float mu2 = n2 > 0 ? __fdividef((float)(kpar * kpar), (float)n2) : 0.f;
         R.add(H, bin, d2, mu2);
         if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
     }
