@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
 k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t rows, int ostride,
               const float2 *__restrict__ g_tw, const float *__restrict__ shift) {
     using CF = RowsCfg<N>;
-    constexpr int P = CF::P, LINE = RegPlan<N>::LINE, H = N / 2 + 1;
+    constexpr int P = CF::P, LINE = RegPlan<N>::LINE16, H = N / 2 + 1;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     const int l = threadIdx.x / P, t = threadIdx.x % P;
@@ -60,13 +60,13 @@ k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t ro
         v[s] = make_float2(a, b);
     }
     __syncthreads();
-    fft_line<N, -1>(v, t, line, tw);
+    fft_line<N, -1, Pad16>(v, t, line, tw);
 #pragma unroll
-    for (int u = 0; u < RegPlan<N>::E; ++u) line[pad8(t + u * P)] = v[u];
+    for (int u = 0; u < RegPlan<N>::E; ++u) line[pad16(t + u * P)] = v[u];
     __syncthreads();
     for (int k = t; k < H; k += P) {
-        const float2 Z = line[pad8(k)];
-        const float2 Zm = line[pad8(k == 0 ? 0 : N - k)];
+        const float2 Z = line[pad16(k)];
+        const float2 Zm = line[pad16(k == 0 ? 0 : N - k)];
         if (ra < rows)
             out[ra * ostride + k] = make_float2(0.5f * (Z.x + Zm.x), 0.5f * (Z.y - Zm.y));
         if (rb < rows)
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(RowsCfg<N>::THREADS, 1)
 k_rows_c2r_p2(const float2 *__restrict__ in, float *__restrict__ out, int64_t rows, int istride,
               const float2 *__restrict__ g_tw, float scale) {
     using CF = RowsCfg<N>;
-    constexpr int P = CF::P, LINE = RegPlan<N>::LINE, H = N / 2 + 1;
+    constexpr int P = CF::P, LINE = RegPlan<N>::LINE16, H = N / 2 + 1;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     const int l = threadIdx.x / P, t = threadIdx.x % P;
@@ -99,7 +99,7 @@ k_rows_c2r_p2(const float2 *__restrict__ in, float *__restrict__ out, int64_t ro
         v[s] = make_float2(A.x - B.y, A.y + B.x);
     }
     __syncthreads();
-    fft_line<N, +1>(v, t, line, tw);
+    fft_line<N, +1, Pad16>(v, t, line, tw);
 #pragma unroll
     for (int u = 0; u < RegPlan<N>::E; ++u) {
         if (ra < rows) out[ra * N + t + u * P] = v[u].x * scale;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(ColsCfg<N>::THREADS, 1)
 k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
           const float2 *__restrict__ g_tw) {
     using CF = ColsCfg<N>;
-    constexpr int P = CF::P, C = CF::C, LINE = RegPlan<N>::LINE;
+    constexpr int P = CF::P, C = CF::C, LINE = RegPlan<N>::LINE8;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(ColsCfg<N>::THREADS, ColsCfg<N>::PK_MINB)
 k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restrict__ g_tw,
           const float *__restrict__ g_win, int axis, int kmax, PkAcc acc, int nitems, int ipb) {
     using CF = ColsCfg<N>;
-    constexpr int P = CF::P, C = CF::C, LINE = RegPlan<N>::LINE;
+    constexpr int P = CF::P, C = CF::C, LINE = RegPlan<N>::LINE8;
     constexpr int MID = N / 2;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
@@ -151,7 +151,7 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
     float2 *line = sm + N + c * LINE;
     float *win = reinterpret_cast<float *>(sm + N + C * LINE);
     FltHist H;
-    H.setup(win + RegPlan<N>::LINE, kmax, MID, WHAT);   // window padded like the lines
+    H.setup(win + LINE, kmax, MID, WHAT);   // window padded like the lines
     for (int i = threadIdx.x; i < N; i += blockDim.x) { tw[i] = g_tw[i]; win[pad8(i)] = g_win[i]; }
     H.zero_all();
     __syncthreads();
@@ -209,7 +209,7 @@ template <int N>
 int rows_r2c_n(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int ostride,
                const float2 *tw, const float *shift) {
     using CF = RowsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * RegPlan<N>::LINE);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * RegPlan<N>::LINE16);
     int st;
     if ((st = set_smem(ctx, k_rows_r2c_p2<N>, smem))) return st;
     const int64_t pairs = (rows + 1) / 2;
@@ -225,7 +225,7 @@ template <int N>
 int rows_c2r_n(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int istride,
                const float2 *tw, float scale) {
     using CF = RowsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * RegPlan<N>::LINE);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::L * RegPlan<N>::LINE16);
     int st;
     if ((st = set_smem(ctx, k_rows_c2r_p2<N>, smem))) return st;
     const int64_t pairs = (rows + 1) / 2;
@@ -241,7 +241,7 @@ template <int N>
 int cols_n(pyl_ctx *ctx, float2 *data, int ncol, int64_t estride, int64_t ostride, int nouter,
            int dir, const float2 *tw) {
     using CF = ColsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE8);
     int st;
     dim3 grid((ncol + CF::C - 1) / CF::C, nouter);
     if (dir < 0) {
@@ -260,8 +260,8 @@ template <int N, int WHAT>
 int pk_n(pyl_ctx *ctx, const float2 *data, int h, int rs, int axis, const float2 *tw,
          const float *win, int kmax, const PkAcc &acc) {
     using CF = ColsCfg<N>;
-    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE) +
-                        sizeof(float) * RegPlan<N>::LINE + FltHist::bytes(kmax, N / 2, WHAT);
+    const size_t smem = sizeof(float2) * (N + (size_t)CF::C * RegPlan<N>::LINE8) +
+                        sizeof(float) * RegPlan<N>::LINE8 + FltHist::bytes(kmax, N / 2, WHAT);
     if (smem > 227 * 1024) return fail(ctx, PYL_ERR_UNSUPPORTED, "Pk histogram too large");
     int st;
     if ((st = set_smem(ctx, k_pk_x_p2<N, WHAT>, smem))) return st;

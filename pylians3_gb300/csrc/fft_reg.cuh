@@ -14,8 +14,12 @@
 // exchange is needed.  Stage radices:
 //   2^k    : one 2 or 4 first when k is not a multiple of 3, then 8s;
 //   3*2^k  : a 3 first, then 4s, then a 2 when k is odd.
-// Shared-memory indices are padded by one element every 8 (pad8) so that
-// the strided stores of the first stage do not conflict on banks.
+// Shared-memory indices are padded (Pad8: one element every 8, Pad16: one
+// every 16) so that the stage exchanges of a half-warp (16 lanes of 8-byte
+// elements) fall on distinct banks.  The row kernels, whose lanes run along
+// one line, use Pad16 (the strided loads read 16 consecutive elements); the
+// column kernels, whose lanes interleave C lines, use Pad8 with a line stride
+// that spreads the lines over the banks (LINE8 / LINE16 below).
 #pragma once
 
 #include "fft_core.cuh"
@@ -29,7 +33,10 @@ struct RegPlan {
     static constexpr bool POW2 = (N & (N - 1)) == 0;
     static constexpr int E = POW2 ? 8 : 12;
     static constexpr int P = N / E;
-    static constexpr int LINE = N + N / 8 + 1;   // padded line stride in shared memory
+    // padded line strides in shared memory (elements): for Pad8 with C
+    // interleaved lines, for Pad16 with lanes along one line
+    static constexpr int LINE8 = N + N / 8 + ((N == 16 || N == 48 || N == 1024 || N == 1536) ? 4 : 2);
+    static constexpr int LINE16 = N + N / 16 + (N == 64 ? 0 : (N == 96 ? 2 : 1));
     static constexpr int K = POW2 ? ilog2c(N) : ilog2c(N / 3);   // power of two part
     static constexpr int NST = POW2 ? (K % 3 == 0 ? K / 3 : K / 3 + 1)
                                     : 1 + K / 2 + (K % 2);
@@ -48,6 +55,13 @@ constexpr bool reg_fft_length() {
 }
 
 __device__ __forceinline__ int pad8(int i) { return i + (i >> 3); }
+__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+struct Pad8 {
+    __device__ __forceinline__ int operator()(int i) const { return pad8(i); }
+};
+struct Pad16 {
+    __device__ __forceinline__ int operator()(int i) const { return pad16(i); }
+};
 
 template <int DIR>
 __device__ __forceinline__ float2 twl(const float2 *tw, int m) {
@@ -115,7 +129,7 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[RegPlan<N>::E], int t,
 }
 
 // Scatter the stage outputs to their Stockham positions in the shared line.
-template <int N, int R, int NS>
+template <int N, int R, int NS, class IDX>
 __device__ __forceinline__ void stage_store(const float2 (&v)[RegPlan<N>::E], int t, float2 *line) {
     constexpr int E = RegPlan<N>::E;
     constexpr int P = RegPlan<N>::P;
@@ -126,22 +140,22 @@ __device__ __forceinline__ void stage_store(const float2 (&v)[RegPlan<N>::E], in
         const int k = j % NS;
         const int ob = (j - k) * R + k;
 #pragma unroll
-        for (int u = 0; u < R; ++u) line[pad8(ob + u * NS)] = v[b + u * NB];
+        for (int u = 0; u < R; ++u) line[IDX()(ob + u * NS)] = v[b + u * NB];
     }
 }
 
-template <int N>
+template <int N, class IDX>
 __device__ __forceinline__ void strided_load(float2 (&v)[RegPlan<N>::E], int t, const float2 *line) {
     constexpr int E = RegPlan<N>::E;
     constexpr int P = RegPlan<N>::P;
 #pragma unroll
-    for (int s = 0; s < E; ++s) v[s] = line[pad8(t + s * P)];
+    for (int s = 0; s < E; ++s) v[s] = line[IDX()(t + s * P)];
 }
 
 // Stage S of the plan (compile-time recursion).  Each exchange between
 // stages is bracketed by __syncthreads(), so every thread of the CTA must
 // call this the same number of times.
-template <int N, int DIR, int S>
+template <int N, int DIR, int S, class IDX>
 __device__ __forceinline__ void run_stages(float2 (&v)[RegPlan<N>::E], int t, float2 *line,
                                            const float2 *tw) {
     using PL = RegPlan<N>;
@@ -149,22 +163,23 @@ __device__ __forceinline__ void run_stages(float2 (&v)[RegPlan<N>::E], int t, fl
     constexpr int NS = PL::ns(S);
     stage_compute<N, R, NS, DIR>(v, t, tw);
     if constexpr (S + 1 < PL::NST) {
-        stage_store<N, R, NS>(v, t, line);
+        stage_store<N, R, NS, IDX>(v, t, line);
         __syncthreads();
-        strided_load<N>(v, t, line);
+        strided_load<N, IDX>(v, t, line);
         __syncthreads();
-        run_stages<N, DIR, S + 1>(v, t, line, tw);
+        run_stages<N, DIR, S + 1, IDX>(v, t, line, tw);
     }
 }
 
-// Full FFT of the thread's line: input and output in the strided layout.
-template <int N, int DIR>
+// Full FFT of the thread's line: input and output in the strided layout;
+// IDX maps line positions to padded shared-memory indices.
+template <int N, int DIR, class IDX = Pad8>
 __device__ __forceinline__ void fft_line(float2 (&v)[RegPlan<N>::E], int t, float2 *line,
                                          const float2 *tw) {
     static_assert(reg_fft_length<N>(), "register FFT length must be 2^k or 3*2^k");
     static_assert(RegPlan<N>::ns(RegPlan<N>::NST - 1) * RegPlan<N>::radix(RegPlan<N>::NST - 1) == N,
                   "stage radices must multiply to N");
-    run_stages<N, DIR, 0>(v, t, line, tw);
+    run_stages<N, DIR, 0, IDX>(v, t, line, tw);
 }
 
 }  // namespace pyl
