@@ -193,6 +193,9 @@ int fft_plane_c2c(pyl_ctx *ctx, float2 *data, int n, int h, int rs, int dir);
 
 // fft_reg.cu: lengths 2^k (16..4096) and 3*2^k (48..3072)
 bool reg_supported(int n);
+// Entries of the register FFT's stage twiddle tables for length n, as
+// indices of the n-entry table (PYL_ERR_UNSUPPORTED if n has no register FFT).
+int reg_stage_twiddle_sources(int n, std::vector<int> &src);
 int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
                   const float2 *tw, const float *shift);
 // total mass (sum of W, or n) into *mass, then *shift = mass / cells

@@ -107,12 +107,19 @@ int stage_flush(pyl_ctx *ctx) {
     return PYL_OK;
 }
 
-// tw[m] = exp(-2 pi i m / n), evaluated in double and rounded to float
+// tw[m] = exp(-2 pi i m / n), evaluated in double and rounded to float, for
+// m < n; for lengths with a register FFT, that FFT's stage tables follow
+// (copies of entries of the first n).
 void twiddles_host(int n, std::vector<float2> &tw) {
     tw.resize(n);
     for (int m = 0; m < n; ++m) {
         const double a = 2.0 * M_PI * (double)m / (double)n;
         tw[m] = make_float2((float)cos(a), (float)(-sin(a)));
+    }
+    std::vector<int> src;
+    if (reg_supported(n) && reg_stage_twiddle_sources(n, src) == PYL_OK) {
+        tw.resize(n + src.size());
+        for (size_t i = 0; i < src.size(); ++i) tw[n + i] = tw[src[i]];
     }
 }
 
@@ -163,9 +170,9 @@ const FftPlan *fft_plan(pyl_ctx *ctx, int n, int *status) {
     factorize(n, P.desc);
     std::vector<float2> tw;
     twiddles_host(n, tw);
-    cudaError_t e = cudaMalloc(&P.d_tw, sizeof(float2) * n);
+    cudaError_t e = cudaMalloc(&P.d_tw, sizeof(float2) * tw.size());
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle table"); return nullptr; }
-    e = cudaMemcpy(P.d_tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(P.d_tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { *status = cuda_fail(ctx, e, "twiddle upload"); return nullptr; }
     return &(g_fft[key] = P);
 }

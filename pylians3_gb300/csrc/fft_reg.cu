@@ -14,6 +14,8 @@
 //                    via a padded shared line; a CTA bins a few items into
 //                    float32 shared histograms and adds them to the float64
 //                    sums when it ends.
+#include <vector>
+
 #include "fft_reg.cuh"
 #include "pk_common.cuh"
 
@@ -49,7 +51,7 @@ k_rows_r2c_p2(const float *__restrict__ in, float2 *__restrict__ out, int64_t ro
     float2 *tw = sm;
     const int l = threadIdx.x / P, t = threadIdx.x % P;
     float2 *line = sm + N + l * LINE;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    load_stage_twiddles<N>(tw, g_tw);
     const float sh = shift ? *shift : 0.f;
     const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
     float2 v[RegPlan<N>::E];
@@ -84,7 +86,7 @@ k_rows_c2r_p2(const float2 *__restrict__ in, float *__restrict__ out, int64_t ro
     float2 *tw = sm;
     const int l = threadIdx.x / P, t = threadIdx.x % P;
     float2 *line = sm + N + l * LINE;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    load_stage_twiddles<N>(tw, g_tw);
     const int64_t ra = 2 * ((int64_t)blockIdx.x * CF::L + l), rb = ra + 1;
     float2 v[RegPlan<N>::E];
 #pragma unroll
@@ -119,7 +121,7 @@ k_cols_p2(float2 *__restrict__ data, int ncol, int64_t estride, int64_t ostride,
     float2 *tw = sm;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
     float2 *line = sm + N + c * LINE;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = g_tw[i];
+    load_stage_twiddles<N>(tw, g_tw);
     const int col = blockIdx.x * C + c;
     const bool valid = col < ncol;
     float2 *base = data + (int64_t)blockIdx.y * ostride + col;
@@ -152,7 +154,8 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
     float *win = reinterpret_cast<float *>(sm + N + C * LINE);
     FltHist H;
     H.setup(win + LINE, kmax, MID, WHAT);   // window padded like the lines
-    for (int i = threadIdx.x; i < N; i += blockDim.x) { tw[i] = g_tw[i]; win[pad8(i)] = g_win[i]; }
+    load_stage_twiddles<N>(tw, g_tw);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) win[pad8(i)] = g_win[i];
     H.zero_all();
     __syncthreads();
     const int nzb = (h + C - 1) / C;
@@ -327,23 +330,25 @@ bool reg_supported(int n) {
         default: return PYL_ERR_UNSUPPORTED;       \
     }
 
+// tw: a table from twiddles_host(n); the kernels read the stage tables
+// appended after its first n entries.
 int pow2_rows_r2c(pyl_ctx *ctx, const float *in, float2 *out, int64_t rows, int n, int ostride,
                   const float2 *tw, const float *shift) {
-#define CALL(N) rows_r2c_n<N>(ctx, in, out, rows, ostride, tw, shift)
+#define CALL(N) rows_r2c_n<N>(ctx, in, out, rows, ostride, tw + N, shift)
     PYL_POW2_DISPATCH(n, CALL)
 #undef CALL
 }
 
 int pow2_rows_c2r(pyl_ctx *ctx, const float2 *in, float *out, int64_t rows, int n, int istride,
                   const float2 *tw, float scale) {
-#define CALL(N) rows_c2r_n<N>(ctx, in, out, rows, istride, tw, scale)
+#define CALL(N) rows_c2r_n<N>(ctx, in, out, rows, istride, tw + N, scale)
     PYL_POW2_DISPATCH(n, CALL)
 #undef CALL
 }
 
 int pow2_cols(pyl_ctx *ctx, float2 *data, int n, int ncol, int64_t estride, int64_t ostride,
               int nouter, int dir, const float2 *tw) {
-#define CALL(N) cols_n<N>(ctx, data, ncol, estride, ostride, nouter, dir, tw)
+#define CALL(N) cols_n<N>(ctx, data, ncol, estride, ostride, nouter, dir, tw + N)
     PYL_POW2_DISPATCH(n, CALL)
 #undef CALL
 }
@@ -351,7 +356,20 @@ int pow2_cols(pyl_ctx *ctx, float2 *data, int n, int ncol, int64_t estride, int6
 int pow2_pk_x(pyl_ctx *ctx, const float2 *data, int n, int rs, int axis, const float2 *tw,
               const float *win, int kmax, const PkAcc &acc, int what) {
     const int h = n / 2 + 1;
-#define CALL(N) pk_what<N>(ctx, data, h, rs, axis, tw, win, kmax, acc, what)
+#define CALL(N) pk_what<N>(ctx, data, h, rs, axis, tw + N, win, kmax, acc, what)
+    PYL_POW2_DISPATCH(n, CALL)
+#undef CALL
+}
+
+template <int N>
+int stage_sources_n(std::vector<int> &src) {
+    src.resize(TwStages<N>::SIZE);
+    for (int i = 0; i < TwStages<N>::SIZE; ++i) src[i] = stage_tw_src<N, 0>(i);
+    return PYL_OK;
+}
+
+int reg_stage_twiddle_sources(int n, std::vector<int> &src) {
+#define CALL(N) stage_sources_n<N>(src)
     PYL_POW2_DISPATCH(n, CALL)
 #undef CALL
 }

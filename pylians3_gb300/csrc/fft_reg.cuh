@@ -48,6 +48,45 @@ struct RegPlan {
     static constexpr int ns(int s) { return s == 0 ? 1 : ns(s - 1) * radix(s - 1); }
 };
 
+// Twiddles of the stages with NS > 1, stage after stage: stage s holds
+// T_s[q * NS + k] = W_N^(m_q * k * ST), k < NS, with m_q = 2^q for q <
+// mults(R) (W^k, W^2k and W^4k for radix 8; W^k, W^2k for radix 4 and 3;
+// W^k for radix 2).  A half-warp then reads consecutive k (or one k by
+// broadcast) instead of k * ST-strided entries of an N-entry table, which
+// fall on few banks.  SIZE < N for every supported length.
+template <int N>
+struct TwStages {
+    using PL = RegPlan<N>;
+    static constexpr int mults(int R) { return R == 8 ? 3 : (R == 2 ? 1 : 2); }
+    static constexpr int count(int s) { return PL::ns(s) > 1 ? mults(PL::radix(s)) * PL::ns(s) : 0; }
+    static constexpr int off(int s) { return s == 0 ? 0 : off(s - 1) + count(s - 1); }
+    static constexpr int SIZE = off(PL::NST);
+    static_assert(SIZE <= N, "stage twiddles fit the N-entry slot");
+};
+
+// Entry i of the stage tables as an index of the N-entry table W_N^m (the
+// host appends the stage tables after that table: twiddles_host).
+template <int N, int S>
+__host__ __device__ inline int stage_tw_src(int i) {
+    if constexpr (S >= RegPlan<N>::NST) {
+        return 0;
+    } else {
+        constexpr int NS = RegPlan<N>::ns(S), R = RegPlan<N>::radix(S), ST = N / (NS * R);
+        constexpr int O0 = TwStages<N>::off(S), O1 = TwStages<N>::off(S + 1);
+        if (O1 > O0 && i >= O0 && i < O1) {
+            const int r = i - O0;
+            return (1 << (r / NS)) * (r % NS) * ST;
+        }
+        return stage_tw_src<N, S + 1>(i);
+    }
+}
+
+// Shared stage tables from their global copy (all threads).
+template <int N>
+__device__ __forceinline__ void load_stage_twiddles(float2 *tw, const float2 *__restrict__ g_stw) {
+    for (int i = threadIdx.x; i < TwStages<N>::SIZE; i += blockDim.x) tw[i] = g_stw[i];
+}
+
 template <int N>
 constexpr bool reg_fft_length() {
     return (N >= 16 && (N & (N - 1)) == 0) ||
@@ -81,13 +120,12 @@ __device__ __forceinline__ void dft3(float2 &a0, float2 &a1, float2 &a2) {
     a2 = csub(m, r);
 }
 
-// One stage in registers.
+// One stage in registers; tw: this stage's table (TwStages).
 template <int N, int R, int NS, int DIR>
 __device__ __forceinline__ void stage_compute(float2 (&v)[RegPlan<N>::E], int t, const float2 *tw) {
     constexpr int E = RegPlan<N>::E;
     constexpr int P = RegPlan<N>::P;
     constexpr int NB = E / R;
-    constexpr int ST = N / (NS * R);   // table stride of W
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = t + b * P;
@@ -97,18 +135,18 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[RegPlan<N>::E], int t,
         for (int q = 0; q < R; ++q) x[q] = v[b + q * NB];
         if constexpr (NS > 1) {
             if constexpr (R == 2) {
-                x[1] = cmul(x[1], twl<DIR>(tw, k * ST));
+                x[1] = cmul(x[1], twl<DIR>(tw, k));
             } else if constexpr (R == 3) {
-                x[1] = cmul(x[1], twl<DIR>(tw, k * ST));
-                x[2] = cmul(x[2], twl<DIR>(tw, 2 * k * ST));
+                x[1] = cmul(x[1], twl<DIR>(tw, k));
+                x[2] = cmul(x[2], twl<DIR>(tw, NS + k));
             } else if constexpr (R == 4) {
-                const float2 w1 = twl<DIR>(tw, k * ST), w2 = twl<DIR>(tw, 2 * k * ST);
+                const float2 w1 = twl<DIR>(tw, k), w2 = twl<DIR>(tw, NS + k);
                 x[1] = cmul(x[1], w1);
                 x[2] = cmul(x[2], w2);
                 x[3] = cmul(x[3], cmul(w1, w2));
             } else {
-                const float2 w1 = twl<DIR>(tw, k * ST), w2 = twl<DIR>(tw, 2 * k * ST);
-                const float2 w4 = twl<DIR>(tw, 4 * k * ST);
+                const float2 w1 = twl<DIR>(tw, k), w2 = twl<DIR>(tw, NS + k);
+                const float2 w4 = twl<DIR>(tw, 2 * NS + k);
                 const float2 w3 = cmul(w1, w2);
                 x[1] = cmul(x[1], w1);
                 x[2] = cmul(x[2], w2);
@@ -161,7 +199,7 @@ __device__ __forceinline__ void run_stages(float2 (&v)[RegPlan<N>::E], int t, fl
     using PL = RegPlan<N>;
     constexpr int R = PL::radix(S);
     constexpr int NS = PL::ns(S);
-    stage_compute<N, R, NS, DIR>(v, t, tw);
+    stage_compute<N, R, NS, DIR>(v, t, tw + TwStages<N>::off(S));
     if constexpr (S + 1 < PL::NST) {
         stage_store<N, R, NS, IDX>(v, t, line);
         __syncthreads();
@@ -172,7 +210,8 @@ __device__ __forceinline__ void run_stages(float2 (&v)[RegPlan<N>::E], int t, fl
 }
 
 // Full FFT of the thread's line: input and output in the strided layout;
-// IDX maps line positions to padded shared-memory indices.
+// IDX maps line positions to padded shared-memory indices; tw holds the
+// stage tables (load_stage_twiddles).
 template <int N, int DIR, class IDX = Pad8>
 __device__ __forceinline__ void fft_line(float2 (&v)[RegPlan<N>::E], int t, float2 *line,
                                          const float2 *tw) {

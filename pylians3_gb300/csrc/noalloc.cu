@@ -86,10 +86,15 @@ extern "C" int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double
     mode_table_init(T, dims, ax, nn, n1, n2);
     const AccLayout L = acc_layout(T);
 
+    std::vector<float2> htw;
+    std::vector<float> hwin;
+    twiddles_host(dims, htw);
+    window_host(dims, mas, hwin);
+
     // carve the scratch array
     size_t off = 0;
     float2 *tw = (float2 *)(base + off);
-    off = align256(off + sizeof(float2) * dims);
+    off = align256(off + sizeof(float2) * htw.size());
     float *win = (float *)(base + off);
     off = align256(off + sizeof(float) * dims);
     unsigned long long *counts = (unsigned long long *)(base + off);
@@ -101,11 +106,7 @@ extern "C" int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double
     if (off > kNoAllocScratchBytes)
         return fail(ctx, PYL_ERR_UNSUPPORTED, "pyl_pk_noalloc: grid does not fit the scratch");
 
-    std::vector<float2> htw;
-    std::vector<float> hwin;
-    twiddles_host(dims, htw);
-    window_host(dims, mas, hwin);
-    PYL_CUDA(ctx, cudaMemcpyAsync(tw, htw.data(), sizeof(float2) * dims, cudaMemcpyHostToDevice,
+    PYL_CUDA(ctx, cudaMemcpyAsync(tw, htw.data(), sizeof(float2) * htw.size(), cudaMemcpyHostToDevice,
                                   ctx->stream));
     PYL_CUDA(ctx, cudaMemcpyAsync(win, hwin.data(), sizeof(float) * dims, cudaMemcpyHostToDevice,
                                   ctx->stream));
