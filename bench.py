@@ -67,6 +67,8 @@ def parse():
                     help="precision mode: extra fraction of particles in Plummer halos")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--out-dir", default=None,
+                    help="precision mode: folder for the per-bin error arrays (.npy)")
     ap.add_argument("--cpu-sample", type=int, default=16,
                     help="CPU baseline runs 1/this of the particles and of the mode loop")
     return ap.parse_args()
@@ -631,8 +633,9 @@ def run_precision(a):
             "max_err_all_bins": float(err.max()),
             "bins_over_1e-4": int((err > 1e-4).sum()),
             "seconds": secs.get(name)}
-        np.save(os.path.join(ROOT, "gpurun_out", "precision_err_%s_%s_%d_h%g.npy"
-                             % (name, a.mas, dims, a.halos)), err)
+        if a.out_dir:
+            np.save(os.path.join(a.out_dir, "precision_err_%s_%s_%d_h%g.npy"
+                                 % (name, a.mas, dims, a.halos)), err)
     line = {"mode": "precision", "metric": "per-bin error of P_ell vs the float64 oracle",
             "unit": "max over ell |dP_ell| / |P_0|, per bin", "bins": int(len(ref.Pk)),
             "nyquist_bin": mid, "variants": rows, "oracle_seconds": t_oracle,
@@ -649,7 +652,8 @@ def main():
     if a.impl == "reference":
         run_reference(a)
     elif a.mode == "precision":
-        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+        if a.out_dir:
+            os.makedirs(a.out_dir, exist_ok=True)
         run_precision(a)
     elif a.mode == "batched":
         run_batched(a)
