@@ -278,9 +278,6 @@ struct TileGeom {
 #ifndef PYL_PART_MINB
 #define PYL_PART_MINB 4
 #endif
-#ifndef PYL_PART_WRITE
-#define PYL_PART_WRITE 1
-#endif
 constexpr int KP = PYL_PART_KP;
 constexpr int kPartThreads = PYL_PART_THREADS;
 static_assert(KP % 4 == 0, "bulk copies move whole 16-byte groups");
@@ -623,10 +620,9 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             }
             if (threadIdx.x < nkeys) gbase[threadIdx.x] = my_base;
             __syncthreads();
-            // key runs are contiguous both here and in the destination
-#if PYL_PART_WRITE == 1
-            // one particle per thread: consecutive threads hold consecutive
-            // slots of a run, so each of the three stores covers one span
+            // key runs are contiguous both here and in the destination; one
+            // particle per thread: consecutive threads hold consecutive slots
+            // of a run, so each of the three stores covers one span
             for (int e = threadIdx.x; e < cs; e += blockDim.x) {
                 const int key = skey2[e];
                 const size_t d = (size_t)gbase[key] + (e - loff[key]);
@@ -636,20 +632,6 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
                 dst[3 * d + 2] = z;
                 if (HAS_W) dstw[d] = sw2[e];
             }
-#else
-            for (int j = threadIdx.x; j < 3 * cs; j += blockDim.x) {
-                const int e = j / 3;
-                const int key = skey2[e];
-                const size_t d = (size_t)gbase[key] + (e - loff[key]);
-                dst[3 * d + (j - 3 * e)] = sp2[j];
-            }
-            if (HAS_W) {
-                for (int e = threadIdx.x; e < cs; e += blockDim.x) {
-                    const int key = skey2[e];
-                    dstw[(size_t)gbase[key] + (e - loff[key])] = sw2[e];
-                }
-            }
-#endif
             __syncthreads();
             seg0 = seg1;
         }
