@@ -34,7 +34,10 @@ struct RegPlan {
     static constexpr int E = POW2 ? 8 : 12;
     static constexpr int P = N / E;
     // padded line strides in shared memory (elements): for Pad8 with C
-    // interleaved lines, for Pad16 with lanes along one line
+    // interleaved lines, for Pad16 with lanes along one line.  The extra
+    // elements per length minimise the bank-conflict wavefronts of all the
+    // exchange accesses (stage stores, strided loads, r2c split, binning
+    // reads), counted per half-warp of 8-byte elements for each length.
     static constexpr int LINE8 = N + N / 8 + ((N == 16 || N == 48 || N == 1024 || N == 1536) ? 4 : 2);
     static constexpr int LINE16 = N + N / 16 + (N == 64 ? 0 : (N == 96 ? 2 : 1));
     static constexpr int K = POW2 ? ilog2c(N) : ilog2c(N / 3);   // power of two part
