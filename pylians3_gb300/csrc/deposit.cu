@@ -842,10 +842,15 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             }
             // A footprint cell takes taps from the home cells of an R^3 box
             // only, so R^3 times the largest home cell bounds every cell.
-            // Where that bound leaves fewer than 21 fractional bits (dense
-            // clumps), the box sums of the histogram give the tight bound.
+            // Where that bound leaves fewer than FAST_BITS fractional bits,
+            // the box sums of the histogram give the tight bound.  TSC and
+            // PCS need 24 bits there: with R^3 = 64 the loose bound costs
+            // them about two bits, and the 512^3 TSC corner bins beyond the
+            // Nyquist wavenumber then moved from 1.4e-4 to 3.8e-4 of P0;
+            // NGP / CIC keep the loose bound from 21 bits on (no change
+            // measured).
             constexpr int R = S::LO + S::HI + 1;
-            constexpr int FAST_BITS = MIN_BITS > 21 ? MIN_BITS : 21;
+            constexpr int FAST_BITS = (MAS == PYL_MAS_TSC || MAS == PYL_MAS_PCS) ? 24 : 21;
             int e = 0;
             fixed = fixed_exponent<MAS, HAS_W>(
                 block_max_nan(HAS_W ? lmf : (float)lmi, s_max) * (float)(R * R * R), e);
