@@ -847,8 +847,8 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             // PCS need 24 bits there: with R^3 = 64 the loose bound costs
             // them about two bits, and the 512^3 TSC corner bins beyond the
             // Nyquist wavenumber then moved from 1.4e-4 to 3.8e-4 of P0;
-            // NGP / CIC keep the loose bound from 21 bits on (no change
-            // measured).
+            // NGP / CIC keep the loose bound from 21 bits on (512^3 CIC:
+            // worst bin 3.0e-6 -> 5.4e-6 of P0).
             constexpr int R = S::LO + S::HI + 1;
             constexpr int FAST_BITS = (MAS == PYL_MAS_TSC || MAS == PYL_MAS_PCS) ? 24 : 21;
             int e = 0;
