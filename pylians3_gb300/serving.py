@@ -64,13 +64,18 @@ class Server:
 
     ``slots``: requests that may be on the device at once.
     ``hbm_budget``: bytes of device memory the slots' workspaces may hold.
+    ``contexts``: the slots' contexts, if the caller builds them (default:
+    ``slots`` new contexts on ``device``); a context needs ``lib``, ``ptr``,
+    ``workspace_bytes()``, ``trim()`` and ``close()``.
     """
 
-    def __init__(self, slots: int = 8, hbm_budget: float = 150e9, device: int = 0):
+    def __init__(self, slots: int = 8, hbm_budget: float = 150e9, device: int = 0,
+                 contexts=None):
         self.device = device
         self.budget = int(hbm_budget)
-        self.ctx = [_native.Context(device) for _ in range(slots)]
-        self.busy: list = [None] * slots
+        self.ctx = (list(contexts) if contexts is not None
+                    else [_native.Context(device) for _ in range(slots)])
+        self.busy: list = [None] * len(self.ctx)
         self.q: deque = deque()
         self.cv = threading.Condition()
         self.running = True
