@@ -80,6 +80,14 @@ def _load():
     lib.orc_pk_bin_d.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                  fp, fp, fp]
     lib.orc_pk_bin_d.restype = None
+    lib.orc_pk_bin_mt.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int] + [fp] * 9
+    lib.orc_pk_bin_mt.restype = None
+    lib.orc_pk_bin_d_mt.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, fp, fp, fp]
+    lib.orc_pk_bin_d_mt.restype = None
+    lib.orc_mode_counts.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [fp] * 5
+    lib.orc_mode_counts.restype = None
     lib.orc_num_threads.restype = ctypes.c_int
     _lib = lib
     return lib
@@ -204,7 +212,10 @@ class Pk:
     """Restatement of class Pk (Pk_library.pyx:263-418)."""
 
     def __init__(self, delta, BoxSize, axis=2, MAS="CIC", threads=1,
-                 verbose=False, delta_k=None, rows=None):
+                 verbose=False, delta_k=None, rows=None, bin_threads=1):
+        """bin_threads != 1 runs the mode loop's rows on that many cores (0:
+        all), private float64 sums added at the end: the same per-mode
+        values, another order of the float64 sums (large test grids)."""
         lib = _load()
         dims = len(delta) if delta is not None else delta_k.shape[0]
         kF, kN, kmax_par, kmax_per, kmax = frequencies(BoxSize, dims)
@@ -222,10 +233,14 @@ class Pk:
         Pkphase = np.zeros(kmax + 1)
         N3D = np.zeros(kmax + 1)
         r0, r1 = (0, dims) if rows is None else rows
-        lib.orc_pk_bin(delta_k.ctypes.data, dims, int(axis), MAS_index, r0, r1,
-                       k1D.ctypes.data, Pk1D.ctypes.data, N1D.ctypes.data,
-                       Pk2D.ctypes.data, N2D.ctypes.data, k3D.ctypes.data,
-                       Pk3D.ctypes.data, Pkphase.ctypes.data, N3D.ctypes.data)
+        outs = (k1D.ctypes.data, Pk1D.ctypes.data, N1D.ctypes.data,
+                Pk2D.ctypes.data, N2D.ctypes.data, k3D.ctypes.data,
+                Pk3D.ctypes.data, Pkphase.ctypes.data, N3D.ctypes.data)
+        if bin_threads != 1 and rows is None:
+            lib.orc_pk_bin_mt(delta_k.ctypes.data, dims, int(axis), MAS_index,
+                              int(bin_threads), *outs)
+        else:
+            lib.orc_pk_bin(delta_k.ctypes.data, dims, int(axis), MAS_index, r0, r1, *outs)
         self.raw = dict(k3D=k3D.copy(), Pk3D=Pk3D.copy(), N3D=N3D.copy())
         if rows is not None:          # bounded sample for timing: no finalisation
             return
@@ -259,11 +274,33 @@ class Pk:
         self.Nmodes3D = N3D
 
 
+def mode_counts(dims, axis=2, threads=0):
+    """Mode counts and k sums of class Pk without the data (the index part of
+    Pk_library.pyx:311-378 on all cores) with the reference's finalisation
+    of k3D / k1D (:384-409): returns dict k3D, Nmodes3D (DC bin dropped),
+    k1D, Nmodes1D, Nmodes2D, as the attributes of class Pk for BoxSize 2 pi
+    (kF = 1)."""
+    lib = _load()
+    kF, kN, kmax_par, kmax_per, kmax = frequencies(2.0 * np.pi, dims)
+    k1D = np.zeros(kmax_par + 1)
+    N1D = np.zeros(kmax_par + 1)
+    N2D = np.zeros((kmax_par + 1) * (kmax_per + 1))
+    k3D = np.zeros(kmax + 1)
+    N3D = np.zeros(kmax + 1)
+    lib.orc_mode_counts(int(dims), int(axis), int(threads), k1D.ctypes.data, N1D.ctypes.data,
+                        N2D.ctypes.data, k3D.ctypes.data, N3D.ctypes.data)
+    if int(np.sum(N3D)) != expected_modes(dims):
+        raise AssertionError("oracle mode count %d != %d" % (int(np.sum(N3D)), expected_modes(dims)))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return dict(k3D=(k3D[1:] / N3D[1:]) * kF, Nmodes3D=N3D[1:],
+                    k1D=(k1D[1:] / N1D[1:]) * kF, Nmodes1D=N1D[1:], Nmodes2D=N2D)
+
+
 class Pk_f64:
     """Float64 precision oracle: float64 FFT of a float64 grid, window and
     sums in float64 (k3D, Pk[:,0:3], Nmodes3D as class Pk)."""
 
-    def __init__(self, delta, BoxSize, axis=2, MAS="CIC", threads=1):
+    def __init__(self, delta, BoxSize, axis=2, MAS="CIC", threads=1, bin_threads=1):
         import scipy.fft as sf
         lib = _load()
         dims = delta.shape[0]
@@ -274,8 +311,13 @@ class Pk_f64:
         k3D = np.zeros(kmax + 1)
         Pk3D = np.zeros((kmax + 1, 3))
         N3D = np.zeros(kmax + 1)
-        lib.orc_pk_bin_d(dk.ctypes.data, dims, int(axis), MAS_function(MAS),
-                         k3D.ctypes.data, Pk3D.ctypes.data, N3D.ctypes.data)
+        if bin_threads != 1:
+            lib.orc_pk_bin_d_mt(dk.ctypes.data, dims, int(axis), MAS_function(MAS),
+                                int(bin_threads), k3D.ctypes.data, Pk3D.ctypes.data,
+                                N3D.ctypes.data)
+        else:
+            lib.orc_pk_bin_d(dk.ctypes.data, dims, int(axis), MAS_function(MAS),
+                             k3D.ctypes.data, Pk3D.ctypes.data, N3D.ctypes.data)
         unit = (BoxSize / dims ** 2) ** 3
         k3D, N3D, Pk3D = k3D[1:], N3D[1:], Pk3D[1:]
         self.k3D = k3D / N3D * kF

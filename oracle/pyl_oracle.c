@@ -18,13 +18,15 @@
  *   orc_deposit_omp                        <- library/MAS_library/MAS_c.c:8-266
  *        (OpenMP particle loop with an atomic add per tap)
  *   orc_pk_bin                             <- library/Pk_library/Pk_library.pyx:311-378
- *        (the independent-mode loop of class Pk)
+ *        (the independent-mode loop of class Pk); orc_pk_bin_mt runs its rows
+ *        on all cores, orc_mode_counts its index part alone (no data)
  * Parity of this file with the compiled reference is pinned by the golden
  * vectors under tests/golden/ (generated by tests/golden/make_golden.py from
  * the reference compiled by oracle/build_ref.py).
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -415,15 +417,128 @@ void orc_pk_bin(const float *dk, int dims, int axis, int MAS_index,
     }
 }
 
+/* The same loop with its kxx rows split over `threads` OpenMP threads (0:
+ * all cores), each summing into private arrays that are added at the end.
+ * Every per-mode value is the serial loop's; only the order of the float64
+ * sums differs (for large grids in tests, where the serial loop is slow).  */
+void orc_pk_bin_mt(const float *dk, int dims, int axis, int MAS_index, int threads,
+                   double *k1D, double *Pk1D, double *N1D,
+                   double *Pk2D, double *N2D,
+                   double *k3D, double *Pk3D, double *Pkphase, double *N3D)
+{
+    const int middle = dims / 2;
+    const long n1 = middle + 1;
+    const long kmax_per = (long)sqrt((double)(2L * middle * middle));
+    const long kmax = (long)sqrt((double)(3L * middle * middle));
+    const long n2 = n1 * (kmax_per + 1), n3 = kmax + 1;
+    const long per = 3 * n1 + 2 * n2 + 6 * n3;   /* doubles per thread */
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#else
+    threads = 1;
+#endif
+    if (threads > dims) threads = dims;
+    double *buf = (double *)calloc((size_t)threads * per, sizeof(double));
+    if (!buf) return;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+#endif
+    for (int t = 0; t < threads; t++) {
+        double *b = buf + (size_t)t * per;
+        const int r0 = (int)((long)dims * t / threads), r1 = (int)((long)dims * (t + 1) / threads);
+        orc_pk_bin(dk, dims, axis, MAS_index, r0, r1, b, b + n1, b + 2 * n1,
+                   b + 3 * n1, b + 3 * n1 + n2, b + 3 * n1 + 2 * n2,
+                   b + 3 * n1 + 2 * n2 + n3, b + 3 * n1 + 2 * n2 + 4 * n3,
+                   b + 3 * n1 + 2 * n2 + 5 * n3);
+    }
+    double *outs[9] = {k1D, Pk1D, N1D, Pk2D, N2D, k3D, Pk3D, Pkphase, N3D};
+    const long lens[9] = {n1, n1, n1, n2, n2, n3, 3 * n3, n3, n3};
+    for (int t = 0; t < threads; t++) {
+        const double *b = buf + (size_t)t * per;
+        for (int a = 0; a < 9; a++) {
+            for (long i = 0; i < lens[a]; i++) outs[a][i] += b[i];
+            b += lens[a];
+        }
+    }
+    free(buf);
+}
+
+/* The index part of the mode loop alone (Pk_library.pyx:318-345, 360-378
+ * without the data): per-bin mode counts N1D, N2D, N3D and the sums of k
+ * (k1D, k3D), over all cores.  The float64 counts are exact integers.     */
+void orc_mode_counts(int dims, int axis, int threads, double *k1D, double *N1D,
+                     double *N2D, double *k3D, double *N3D)
+{
+    const int middle = dims / 2;
+    const int kmax_par = middle;
+    const long n1 = middle + 1;
+    const long kmax_per = (long)sqrt((double)(2L * middle * middle));
+    const long kmax = (long)sqrt((double)(3L * middle * middle));
+    const long n2 = n1 * (kmax_per + 1), n3 = kmax + 1;
+    const long per = 2 * n1 + n2 + 2 * n3;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#else
+    threads = 1;
+#endif
+    if (threads > dims) threads = dims;
+    double *buf = (double *)calloc((size_t)threads * per, sizeof(double));
+    if (!buf) return;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+#endif
+    for (int t = 0; t < threads; t++) {
+        double *bk1 = buf + (size_t)t * per, *bn1 = bk1 + n1, *bn2 = bn1 + n1;
+        double *bk3 = bn2 + n2, *bn3 = bk3 + n3;
+        const int r0 = (int)((long)dims * t / threads), r1 = (int)((long)dims * (t + 1) / threads);
+        for (int kxx = r0; kxx < r1; kxx++) {
+            int kx = (kxx > middle) ? kxx - dims : kxx;
+            for (int kyy = 0; kyy < dims; kyy++) {
+                int ky = (kyy > middle) ? kyy - dims : kyy;
+                for (int kzz = 0; kzz < middle + 1; kzz++) {
+                    int kz = (kzz > middle) ? kzz - dims : kzz;
+                    if (kz == 0 || (kz == middle && dims % 2 == 0)) {
+                        if (kx < 0) continue;
+                        else if (kx == 0 || (kx == middle && dims % 2 == 0)) {
+                            if (ky < 0.0) continue;
+                        }
+                    }
+                    double k = sqrt((double)(kx*kx + ky*ky + kz*kz));
+                    int k_index = (int)k;
+                    int k_par, k_per;
+                    if (axis == 0)      { k_par = kx; k_per = (int)sqrt((double)(ky*ky + kz*kz)); }
+                    else if (axis == 1) { k_par = ky; k_per = (int)sqrt((double)(kx*kx + kz*kz)); }
+                    else                { k_par = kz; k_per = (int)sqrt((double)(kx*kx + ky*ky)); }
+                    if (k_par < 0) k_par = -k_par;
+                    if (k <= middle) {
+                        bk1[k_par] += k_par;
+                        bn1[k_par] += 1.0;
+                    }
+                    bn2[(kmax_par + 1) * k_per + k_par] += 1.0;
+                    bk3[k_index] += k;
+                    bn3[k_index] += 1.0;
+                }
+            }
+        }
+    }
+    for (int t = 0; t < threads; t++) {
+        const double *b = buf + (size_t)t * per;
+        for (long i = 0; i < n1; i++) { k1D[i] += b[i]; N1D[i] += b[n1 + i]; }
+        for (long i = 0; i < n2; i++) N2D[i] += b[2 * n1 + i];
+        for (long i = 0; i < n3; i++) { k3D[i] += b[2 * n1 + n2 + i]; N3D[i] += b[2 * n1 + n2 + n3 + i]; }
+    }
+    free(buf);
+}
+
 /* Same loop in float64 throughout for the precision oracle: dk is complex128
- * and the window is applied in double.                                     */
-void orc_pk_bin_d(const double *dk, int dims, int axis, int MAS_index,
-                  double *k3D, double *Pk3D, double *N3D)
+ * and the window is applied in double.  Rows [row0, row1) of kxx.         */
+static void pk_bin_d_rows(const double *dk, int dims, int axis, int MAS_index,
+                          int row0, int row1, double *k3D, double *Pk3D, double *N3D)
 {
     const int middle = dims / 2;
     const int h = middle + 1;
     const double prefact = M_PI / dims;
-    for (int kxx = 0; kxx < dims; kxx++) {
+    for (int kxx = row0; kxx < row1; kxx++) {
         int kx = (kxx > middle) ? kxx - dims : kxx;
         double c0 = mas_correction(prefact * kx, MAS_index);
         for (int kyy = 0; kyy < dims; kyy++) {
@@ -455,6 +570,42 @@ void orc_pk_bin_d(const double *dk, int dims, int axis, int MAS_index,
             }
         }
     }
+}
+
+void orc_pk_bin_d(const double *dk, int dims, int axis, int MAS_index,
+                  double *k3D, double *Pk3D, double *N3D)
+{
+    pk_bin_d_rows(dk, dims, axis, MAS_index, 0, dims, k3D, Pk3D, N3D);
+}
+
+/* orc_pk_bin_d with the kxx rows over `threads` OpenMP threads (0: all). */
+void orc_pk_bin_d_mt(const double *dk, int dims, int axis, int MAS_index, int threads,
+                     double *k3D, double *Pk3D, double *N3D)
+{
+    const int middle = dims / 2;
+    const long n3 = (long)sqrt((double)(3L * middle * middle)) + 1;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#else
+    threads = 1;
+#endif
+    if (threads > dims) threads = dims;
+    double *buf = (double *)calloc((size_t)threads * 5 * n3, sizeof(double));
+    if (!buf) return;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+#endif
+    for (int t = 0; t < threads; t++) {
+        double *b = buf + (size_t)t * 5 * n3;
+        const int r0 = (int)((long)dims * t / threads), r1 = (int)((long)dims * (t + 1) / threads);
+        pk_bin_d_rows(dk, dims, axis, MAS_index, r0, r1, b, b + n3, b + 4 * n3);
+    }
+    for (int t = 0; t < threads; t++) {
+        const double *b = buf + (size_t)t * 5 * n3;
+        for (long i = 0; i < n3; i++) { k3D[i] += b[i]; N3D[i] += b[4 * n3 + i]; }
+        for (long i = 0; i < 3 * n3; i++) Pk3D[i] += b[n3 + i];
+    }
+    free(buf);
 }
 
 int orc_num_threads(void)

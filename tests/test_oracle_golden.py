@@ -70,6 +70,38 @@ def test_mode_counts_match_reference(golden, oracle, dims):
     assert int(r.Nmodes3D.sum()) + 1 == oracle.expected_modes(dims)
 
 
+@pytest.mark.parametrize("dims", [8, 9, 63, 64, 128, 192, 256])
+def test_data_free_mode_counts_match_reference(golden, oracle, dims):
+    """oracle.mode_counts (the index part of the mode loop on all cores, the
+    source of the 512 / 1024 known answers) against the reference's counts."""
+    g = golden["nmodes"]
+    m = oracle.mode_counts(dims, axis=2)
+    assert np.array_equal(m["Nmodes3D"], g["Nmodes3D_d%d" % dims])
+    assert np.array_equal(m["Nmodes1D"], g["Nmodes1D_d%d" % dims])
+    assert np.array_equal(m["Nmodes2D"], g["Nmodes2D_d%d" % dims])
+    np.testing.assert_allclose(m["k3D"] * (2 * np.pi / BOX), g["k3D_d%d" % dims], rtol=1e-12)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_threaded_binning_matches_serial(golden, oracle, axis):
+    """The mode loop with its rows on several cores gives the serial loop's
+    spectra (float64 sums in another order) and the same counts."""
+    delta = golden["pk"]["delta_d24"]
+    a = oracle.Pk(delta, BOX, axis=axis, MAS="TSC")
+    b = oracle.Pk(delta, BOX, axis=axis, MAS="TSC", bin_threads=3)
+    for k in ("Nmodes3D", "Nmodes1D", "Nmodes2D"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    for k in ("k3D", "Pk", "k1D", "Pk1D", "Pkphase"):
+        np.testing.assert_allclose(getattr(b, k), getattr(a, k), rtol=1e-12, atol=0)
+    fin = np.isfinite(a.Pk2D)
+    np.testing.assert_allclose(b.Pk2D[fin], a.Pk2D[fin], rtol=1e-12)
+    d64 = delta.astype(np.float64)
+    c = oracle.Pk_f64(d64, BOX, axis=axis, MAS="TSC")
+    d = oracle.Pk_f64(d64, BOX, axis=axis, MAS="TSC", bin_threads=3)
+    np.testing.assert_allclose(d.Pk, c.Pk, rtol=1e-12)
+    assert np.array_equal(c.Nmodes3D, d.Nmodes3D)
+
+
 def test_pipeline_matches_reference(golden, oracle):
     g = golden["pipeline"]
     dims = g["delta"].shape[0]
