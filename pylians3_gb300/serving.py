@@ -79,6 +79,7 @@ class Server:
         self.q: deque = deque()
         self.cv = threading.Condition()
         self.running = True
+        self.failure = None          # set when the dispatcher dies: no more requests
         self.done_latencies: list = []
         self.completed = 0
         self.thread = threading.Thread(target=self._loop, name="pyl-server", daemon=True)
@@ -105,6 +106,8 @@ class Server:
             raise _native.PylError(_native.PYL_ERR_BUDGET,
                                    "request needs %d bytes, budget %d" % (nbytes, self.budget))
         fut = Future()
+        if self.failure is not None:
+            raise RuntimeError("the server's dispatcher stopped: %r" % (self.failure,))
         r = _Request(pos=pos, n=n, W=W, dims=int(dims), box=float(BoxSize),
                      mas=_native.MAS_CODE[MAS], axis=int(axis),
                      window=MAS_function(MAS if window is None else window), what=int(what),
@@ -112,6 +115,8 @@ class Server:
                      t_submit=time.perf_counter(), t_start=None, t_done=None, bytes=nbytes,
                      out=None, keep=None)
         with self.cv:
+            if self.failure is not None:
+                raise RuntimeError("the server's dispatcher stopped: %r" % (self.failure,))
             self.q.append(r)
             self.cv.notify()
         return fut
@@ -161,10 +166,10 @@ class Server:
         r = self.busy[slot]
         c = self.ctx[slot]
         rc = c.lib.pyl_pk_collect(c.ptr, ctypes.byref(r.out.struct), -1)
-        self.busy[slot] = None
         r.t_done = time.perf_counter()
         if rc != _native.PYL_OK:
             msg = c.lib.pyl_last_error(c.ptr)
+            self.busy[slot] = None
             r.future.set_exception(_native.PylError(rc, msg.decode() if msg else ""))
             return
         res = _Result()
@@ -173,9 +178,29 @@ class Server:
         res.service = r.t_done - r.t_start
         self.done_latencies.append(res.latency)
         self.completed += 1
+        self.busy[slot] = None     # cleared last: a failure above leaves r in busy
         r.future.set_result(res)
 
     def _loop(self):
+        try:
+            self._dispatch()
+        except BaseException as e:   # noqa: BLE001 -- every future must learn of it
+            self._fail_all(e)
+
+    def _fail_all(self, exc):
+        """The dispatcher died: every request in flight or queued fails with
+        the exception, and submit() refuses new requests."""
+        with self.cv:
+            self.failure = exc
+            self.running = False
+            pending = [r for r in self.busy if r is not None] + list(self.q)
+            self.q.clear()
+            self.busy = [None] * len(self.ctx)
+        for r in pending:
+            if not r.future.done():
+                r.future.set_exception(exc)
+
+    def _dispatch(self):
         while True:
             progressed = False
             for i, r in enumerate(self.busy):

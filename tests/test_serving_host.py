@@ -1,6 +1,7 @@
 """Host logic of the continuous-batching server, on the CPU: arrival-order
 admission, the HBM budget (with idle slots trimmed first), error
-propagation and draining on close.  The slots are fake contexts whose
+propagation, draining on close, and a dispatcher that dies (every future
+fails, new submissions are refused).  The slots are fake contexts whose
 "device work" completes after a few polls; no GPU is touched (the library
 is loaded only for its host-side mode-count sizes)."""
 import ctypes
@@ -30,6 +31,8 @@ class _FakeLib:
 
     def pyl_pk_query(self, ptr):
         n, left = self.o.pending
+        if n == 666:                      # a fault inside the dispatcher
+            raise OSError("fake query fault")
         gate = self.o.gates.get(n)
         if gate is not None and not gate.is_set():   # held by the test
             return 0
@@ -164,3 +167,18 @@ def test_invalid_scheme_is_rejected():
     with pytest.raises(ValueError):
         srv.submit(_pos(10), 16, 1000.0, "XYZ")
     srv.close()
+
+
+def test_dispatcher_failure_fails_every_future():
+    gate = threading.Event()
+    srv, _, _, _ = _server(slots=2, budget=150e9, gates={70: gate})
+    held = srv.submit(_pos(70), 16, 1000.0, "CIC")      # in flight, held by the gate
+    boom = srv.submit(_pos(666), 16, 1000.0, "CIC")     # its poll raises
+    queued = [srv.submit(_pos(80 + i), 16, 1000.0, "CIC") for i in range(4)]
+    for f in [held, boom] + queued:
+        with pytest.raises(OSError, match="fake query fault"):
+            f.result(timeout=10)
+    with pytest.raises(RuntimeError, match="dispatcher stopped"):
+        srv.submit(_pos(90), 16, 1000.0, "CIC")
+    gate.set()
+    srv.close(wait=True)                  # returns: the loop has ended
