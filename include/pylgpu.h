@@ -205,9 +205,12 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms);
  * library holds until the process exits.  The first call on a device looks
  * up that array's address (make it before any stream capture).  Calls share
  * the array and it keeps the last call's contents (the sums are cleared on
- * every call); calls that overlap on the GPU race, so issue them one after
- * another.  Nothing is allocated on the device, by this call or the context
- * (create the context with a caller stream so that it makes no stream).    */
+ * every call; the FFT and window tables of the last dims and scheme are
+ * kept, so a call repeating them uploads nothing); calls that overlap on the
+ * GPU race, so issue them one after another.  The call itself allocates no
+ * device memory.  The context does once, when it is created: a 16-byte
+ * device status word (and a stream unless the caller passes one), so create
+ * it before the region where allocation is not allowed.                   */
 int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double BoxSize,
                    int axis, int mas, int what, pyl_pk_out *out);
 

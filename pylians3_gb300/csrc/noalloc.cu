@@ -20,9 +20,15 @@
 //    (cudaGetSymbolAddress) with that device current; make that first call
 //    before any stream capture.
 //  * All calls share the one array and it keeps the last call's contents;
-//    the sums are cleared at the start of every call.  Calls that overlap on
-//    the GPU (other streams, other host threads) race on it: issue them one
-//    after another.
+//    the sums are cleared at the start of every call.  The FFT twiddles and
+//    the window of the last (dims, scheme) stay in the array: a call with the
+//    same dims and scheme as the previous call on that device uploads
+//    nothing.  Calls that overlap on the GPU (other streams, other host
+//    threads) race on it: issue them one after another.
+//  * The call allocates no device memory.  The context it runs on does: its
+//    creation allocates a 16-byte device status word (and a stream, unless
+//    the caller passes one), so create the context once, before the
+//    allocation-free region.
 //  * delta is a device pointer; the outputs are host arrays, as for pyl_pk.
 #include <map>
 #include <mutex>
@@ -38,6 +44,7 @@ namespace {
 
 std::mutex g_mu;
 std::map<int, unsigned char *> g_scratch_addr;             // device -> array address
+std::map<int, std::pair<int, int>> g_tables_in_scratch;    // device -> (dims, mas) uploaded
 std::map<std::pair<int, int>, pyl::ModeTables> g_tables;  // (dims, axis) -> host tables
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -88,7 +95,7 @@ extern "C" int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double
 
     std::vector<float2> htw;
     std::vector<float> hwin;
-    twiddles_host(dims, htw);
+    twiddles_host(dims, htw);   // its size also fixes the scratch layout
     window_host(dims, mas, hwin);
 
     // carve the scratch array
@@ -106,10 +113,28 @@ extern "C" int pyl_pk_noalloc(pyl_ctx *ctx, const float *delta, int dims, double
     if (off > kNoAllocScratchBytes)
         return fail(ctx, PYL_ERR_UNSUPPORTED, "pyl_pk_noalloc: grid does not fit the scratch");
 
-    PYL_CUDA(ctx, cudaMemcpyAsync(tw, htw.data(), sizeof(float2) * htw.size(), cudaMemcpyHostToDevice,
-                                  ctx->stream));
-    PYL_CUDA(ctx, cudaMemcpyAsync(win, hwin.data(), sizeof(float) * dims, cudaMemcpyHostToDevice,
-                                  ctx->stream));
+    // The tables depend on (dims, mas) only and sit at offsets that depend
+    // on dims only: skip the upload when the previous call on this device
+    // left the same ones (calls are issued one after another).
+    const int key_mas = (mas >= 1 && mas <= 4) ? mas : 0;
+    bool tables_current = false;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        auto it = g_tables_in_scratch.find(ctx->device);
+        tables_current = it != g_tables_in_scratch.end() &&
+                         it->second == std::make_pair(dims, key_mas);
+        g_tables_in_scratch.erase(ctx->device);   // re-set once the upload is issued
+    }
+    if (!tables_current) {
+        PYL_CUDA(ctx, cudaMemcpyAsync(tw, htw.data(), sizeof(float2) * htw.size(),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        PYL_CUDA(ctx, cudaMemcpyAsync(win, hwin.data(), sizeof(float) * dims,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        g_tables_in_scratch[ctx->device] = std::make_pair(dims, key_mas);
+    }
 
     // mode tables: counted once per (dims, axis) on the device, kept on the host
     bool have = false;
