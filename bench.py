@@ -7,15 +7,27 @@ binning, and the float64 per-bin sums back on the host (k3D, Pk[:,0:3],
 Nmodes3D) -- pyl_pk_particles, the reference's canonical
 MA -> delta/mean-1 -> Pk caller (Pk_snapshot.py:81-89) in one call.
 
-  value  spectra/s with the positions resident in HBM (device-timed).
-  e2e    the same metric through the public API power_spectrum() with the
-         positions in pinned host memory: every step copies them to the
-         device and reads the spectrum back.
-  roofline  the dominant kernel's algorithmic bytes per launch / its mean
-         CUDA-event duration, against the measured HBM copy bandwidth.
-  cpu_baseline  the reference's CPU path (oracle port: OpenMP atomic deposit
-         as MAS_c.c, scipy FFT on all cores as FFTW threads, the serial mode
-         loop of Pk) on a bounded sample of the same workload.
+  value     spectra/s with the positions resident in HBM (device-timed).
+  e2e       the same metric through the public API with the positions in
+            pinned host memory: every step copies them to the device and
+            reads the spectrum back (power_spectra, two sets in flight).
+  roofline  one whole spectrum: the algorithmic bytes of the hot path per
+            spectrum (12 n + 4 d^3 + 4 d^3 + 16 d^2 (d/2+1): positions read
+            once, grid written once and read once, half-complex grid written
+            once and read once; the sort counts as no useful bytes) over the
+            CUDA-event time of a step, against the measured HBM copy
+            bandwidth.  `stages` breaks it down per stage.
+  headline  the metric's comparison on one request stream of 512^3 CIC
+            spectra from host memory: the plain path (the drop-in MA, numpy
+            delta/mean - 1 and the drop-in Pk, one request at a time, as
+            Pk_snapshot.py:66-89 does) against the batched (power_spectra)
+            and served (serving.Server) forms, with p50/p99 latency.
+  batched   64 realizations of uneven size (dims 128..384): one at a time vs
+            one CUDA-graph launch vs the server.
+  served    Poisson request streams of the mixed served workload.
+  cpu_baseline  one full spectrum of the reference's own CPU code (compiled
+            for this machine from oracle/_ref/kit: serial MA, overdensity,
+            Pk on all cores), or of the oracle port where it is unavailable.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun (N > 1) every rank runs its own replica (no data exchange);
@@ -69,8 +81,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--out-dir", default=None,
                     help="precision mode: folder for the per-bin error arrays (.npy)")
-    ap.add_argument("--cpu-sample", type=int, default=16,
-                    help="CPU baseline runs 1/this of the particles and of the mode loop")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave the headline, batched and served sub-objects out")
+    ap.add_argument("--headline-requests", type=int, default=16,
+                    help="requests in the headline stream (plain vs batched vs served)")
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="reference arm: seconds of timed full spectra (at least one)")
     return ap.parse_args()
 
 
@@ -186,22 +202,35 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def spectrum_bytes(dims, n, weighted=False):
+    """Algorithmic HBM bytes of one spectrum: positions (and weights) read
+    once, the grid written once and read once, the half-complex grid written
+    once and read once (a two-pass FFT lower bound).  Bins and the sort are
+    left out: the sort moves no useful bytes."""
+    h = dims // 2 + 1
+    return n * (12 + (4 if weighted else 0)) + 8 * dims ** 3 + 16 * dims * dims * h
+
+
 def stage_bytes(stage, dims, n, weighted):
-    """Algorithmic HBM bytes per launch of each stage."""
+    """(useful, moved) HBM bytes per launch of each stage.  useful: the
+    stage's share of spectrum_bytes (they add up to it); moved: the least
+    traffic of the stage as built (e.g. the y pass reads and writes the
+    half-complex grid, the sort reads and writes every record)."""
     h = dims // 2 + 1
     real = 4 * dims ** 3
     half = 8 * dims * dims * h
     rec = n * (12 + (4 if weighted else 0))   # one particle record (+ weight)
     return {
-        "tile_count": n * 12,        # read positions
-        "partition": 2 * rec,        # read + write every record once (a one-pass partition)
-        "deposit": rec + real,       # read the sorted records, write the grid once
-        "mass": n * 4 if weighted else 0,
-        "fft_z": real + half,        # read real grid, write half-complex
-        "fft_y": 2 * half,           # read + write
-        "pk_x": half,                # read only (spectrum not stored)
-        "zero": real,
-    }.get(stage)
+        "tile_count": (0, n * 12),       # counting pass of the sort
+        "partition": (0, 4 * rec),       # two passes, each reads and writes every record
+        "deposit": (rec + real, rec + real),
+        "mass": (0, n * 4 if weighted else 0),
+        "zero": (0, real),
+        "fft_z": (real + half, real + half),
+        "fft_y": (0, 2 * half),
+        "pk_x": (half, half),            # read only (the spectrum is not stored)
+        "h2d": (0, 0), "d2h": (0, 0),
+    }.get(stage, (0, 0))
 
 
 def traffic_table():
@@ -217,37 +246,57 @@ def traffic_table():
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_sample(a, pos_np, threads):
-    """Reference CPU path on a bounded sample: returns seconds per spectrum
-    (extrapolated) and a description."""
+def reference_modules():
+    """The reference's own MAS_library and Pk_library compiled for this
+    machine (oracle/_ref; built from oracle/_ref/kit with gcc on first use),
+    or (None, reason)."""
+    try:
+        from oracle import build_ref
+        if not build_ref.built():
+            if not build_ref.have_kit():
+                return None, "no reference compile kit in oracle/_ref/kit"
+            build_ref.build_from_kit()
+        return build_ref.load(), None
+    except Exception as e:  # the CPU baseline falls back to the oracle port
+        return None, "reference build unavailable: %s" % str(e).splitlines()[0][:200]
+
+
+def cpu_spectrum(a, pos_np, threads, mods):
+    """One full spectrum of the reference's CPU path on all particles: a new
+    grid, MA (serial by construction), delta /= mean; delta -= 1 and Pk on
+    `threads` cores -- the sequence of Pk_snapshot.py:66-89.  mods: the
+    compiled reference (MAS_library, Pk_library) or None for the oracle
+    port.  Returns (seconds, per-step seconds)."""
     import numpy as np
-    from oracle import oracle as orc
-    dims, S = a.dims, a.cpu_sample
-    n = pos_np.shape[0]
-    ns = n // S
-    grid = np.zeros((dims,) * 3, np.float32)
+    dims = a.dims
     t0 = time.perf_counter()
-    orc.deposit_omp(a.mas, pos_np[:ns], grid, BOX, threads=threads)
-    t_dep = (time.perf_counter() - t0) * S
-    # the sampled grid stands in for the full one in the steps below
-    t0 = time.perf_counter()
-    grid /= np.mean(grid, dtype=np.float64)
-    grid -= 1.0
-    t_norm = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    dk = orc.FFT3Dr_f(grid, threads)
-    t_fft = time.perf_counter() - t0
-    rows = max(1, dims // S)
-    t0 = time.perf_counter()
-    orc.Pk(None, BOX, axis=a.axis, MAS=a.mas, delta_k=dk, rows=(0, rows))
-    t_bin = (time.perf_counter() - t0) * dims / rows
-    total = t_dep + t_norm + t_fft + t_bin
-    desc = ("oracle port on %d threads: OpenMP atomic deposit of 1/%d of the particles "
-            "(x%d), overdensity + scipy r2c FFT of the full grid, serial mode loop over "
-            "%d of %d kx planes (x%d); per-spectrum %.2f s = deposit %.2f + norm %.2f + "
-            "fft %.2f + bin %.2f" % (threads, S, S, rows, dims, dims // rows, total, t_dep,
-                                     t_norm, t_fft, t_bin))
-    return total, desc
+    delta = np.zeros((dims,) * 3, np.float32)
+    if mods is not None:
+        mods[0].MA(pos_np, delta, BOX, a.mas)
+    else:
+        from oracle import oracle as orc
+        orc.MA(pos_np, delta, BOX, a.mas)
+    t1 = time.perf_counter()
+    mean = pos_np.shape[0] * 1.0 / dims ** 3
+    delta /= mean
+    delta -= 1.0
+    t2 = time.perf_counter()
+    if mods is not None:
+        mods[1].Pk(delta, BOX, a.axis, a.mas, threads, False)
+    else:
+        from oracle import oracle as orc
+        orc.Pk(delta, BOX, axis=a.axis, MAS=a.mas, threads=threads)
+    t3 = time.perf_counter()
+    return t3 - t0, {"ma": t1 - t0, "overdensity": t2 - t1, "pk": t3 - t2}
+
+
+def cpu_kind(mods, why):
+    if mods is not None:
+        return "reference", ("the reference's MAS_library.MA (serial) + delta/mean - 1 + "
+                             "Pk_library.Pk(threads=all cores), compiled for this machine "
+                             "with setup.py's flags; pyFFTW replaced by scipy.fft (absent)")
+    return "port", ("oracle port (%s): serial MA restatement + delta/mean - 1 + Pk "
+                    "restatement, scipy FFT on all cores" % why)
 
 
 def host_positions(a, seed=1234):
@@ -261,29 +310,46 @@ def host_positions(a, seed=1234):
 
 # ----------------------------------------------------------------- arms
 def run_reference(a):
+    """The reference's own CPU path on the same workload: full spectra (all
+    particles, every mode), all host cores for Pk.  At most one warm-up
+    spectrum, then full spectra until --ref-budget seconds are used (at
+    least one): `steps` is the number timed."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from oracle import oracle as orc
-    orc.build()
+    import numpy as np
     threads = os.cpu_count() or 1
+    mods, why = reference_modules()
+    if mods is None:
+        from oracle import oracle as orc
+        orc.build()
+    kind, desc = cpu_kind(mods, why)
     pos = host_positions(a)
-    times = []
-    desc = ""
-    for i in range(a.warmup + a.steps):
-        t, desc = cpu_sample(a, pos, threads)
-        if i >= a.warmup:
-            times.append(t)
+    warm = min(a.warmup, 1)
+    for _ in range(warm):
+        cpu_spectrum(a, pos, threads, mods)
+    times, parts = [], []
+    while len(times) < max(1, a.steps):
+        t, part = cpu_spectrum(a, pos, threads, mods)
+        times.append(t)
+        parts.append(part)
+        if sum(times) >= a.ref_budget:
+            break
     sec = sum(times) / len(times)
     value = 1.0 / sec
+    split = {k: statistics.mean(p[k] for p in parts) for k in parts[0]}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "n_gpus": a.gpus, "steps": len(times), "warmup": warm,
+        "steps_requested": a.steps, "warmup_requested": a.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform positions)",
         "config": workload(a),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "%d full spectra (all %d particles, all modes); %s; "
+                                   "seconds per spectrum: MA %.2f, overdensity %.2f, Pk %.2f"
+                                   % (len(times), a.particles, desc, split["ma"],
+                                      split["overdensity"], split["pk"])},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -350,34 +416,52 @@ def run_ours(a):
     e1.synchronize()
     clk = clocks.stop()
     launches = ctx.launches() - l0
-    stages = ctx.stage_times(reset=True)
+    stages_raw = ctx.stage_times(reset=True)
     ctx.set_timing(False)
     barrier()
     ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     ms_step = ms / a.steps
     value = job_rate(world, a.steps, ms / 1e3)
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of one whole spectrum, and per stage
     peak, peak_kind = peaks()
-    kern = {k: v for k, v in stages.items() if k not in ("h2d", "d2h")}
-    dom = max(kern, key=lambda k: kern[k][0])
-    dom_ms = kern[dom][0] / kern[dom][1]
-    algo = stage_bytes(dom, a.dims, a.particles, False)
-    achieved = algo / (dom_ms / 1e3) / 1e9
-    tr = traffic_table().get((dom, "%s_%d_%s" % (a.mas, a.dims, a.positions)))
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+    weighted = False
+    algo = spectrum_bytes(a.dims, a.particles, weighted)
+    achieved = algo / (ms_step / 1e3) / 1e9
+    tr_tab = traffic_table()
+    key = "%s_%d_%s" % (a.mas, a.dims, a.positions)
+    stages = {}
+    for name, (tot, cnt) in stages_raw.items():
+        useful, moved = stage_bytes(name, a.dims, a.particles, weighted)
+        ms_st = tot / a.steps
+        row = {"ms_per_step": ms_st, "launches_per_step": cnt / a.steps,
+               "useful_bytes": useful, "moved_bytes": moved,
+               "traffic": tr_tab.get((name, key))}
+        if ms_st > 0:
+            row["frac_useful"] = useful / (ms_st / 1e3) / 1e9 / peak
+            row["frac_moved"] = moved / (ms_st / 1e3) / 1e9 / peak
+        stages[name] = row
+    traffic = None
+    if all(tr_tab.get((k, key)) for k in ("tile_count", "partition", "deposit", "fft_z", "fft_y",
+                                           "pk_x")):
+        traffic = sum(v for (st, wk), v in tr_tab.items() if wk == key)
+    one_pass = a.particles * 12 + 8 * a.dims ** 3
+    roof = {"bound": "hbm", "kernel": "one spectrum (all kernels of a step)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)")
             if peak_kind == "measured" else "fallback 6.8 TB/s",
-            "traffic": tr, "algorithmic_bytes_per_launch": algo, "ms_per_launch": dom_ms}
-    h = a.dims // 2 + 1
-    pipe_bytes = (a.particles * 12 + 4 * a.dims ** 3 + 4 * a.dims ** 3 + 2 * 8 * a.dims ** 2 * h)
-    stage_ms = {k: v[0] / a.steps for k, v in stages.items()}
+            "traffic": traffic, "algorithmic_bytes_per_spectrum": algo,
+            "ms_per_spectrum": ms_step,
+            "one_pass_bytes": one_pass,
+            "one_pass_frac": one_pass / (ms_step / 1e3) / 1e9 / peak}
 
     # ---- end to end through the public API with pinned host positions
     e2e = None
-    if not a.no_e2e:
+    host = None
+    if not a.no_e2e or (not a.no_extras and world == 1):
         host = P.pinned_empty((a.particles, 3), np.float32)
         host[...] = pos.cpu().numpy()
+    if not a.no_e2e:
         for _ in range(2):
             P.power_spectrum(host, a.dims, BOX, a.mas, axis=a.axis, ctx=ctx)
         barrier()
@@ -402,18 +486,30 @@ def run_ours(a):
                "api": "pylians3_gb300.power_spectra, pinned host positions, 2 sets in flight",
                "single_call_value": job_rate(world, a.steps, single),
                "single_call_api": "pylians3_gb300.power_spectrum, one call at a time"}
+
+    headline = batched = served = None
+    if not a.no_extras and world == 1:
+        headline = headline_stream(a, P, host, value)
         del host
+        host = None
+        batched = batched_summary(a)
+        served = served_summary(a)
+    del host
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        from oracle import oracle as orc
-        orc.build()
         threads = os.cpu_count() or 1
+        mods, why = reference_modules()
+        if mods is None:
+            from oracle import oracle as orc
+            orc.build()
+        kind, desc = cpu_kind(mods, why)
         pos_np = pos.cpu().numpy()
-        cpu_sample(a, pos_np, threads)   # warm-up (page faults, thread pools)
-        t, desc = cpu_sample(a, pos_np, threads)
-        cpu = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": desc}
+        t, part = cpu_spectrum(a, pos_np, threads, mods)
+        cpu = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": "one full spectrum (all %d particles, all modes); %s; seconds: MA "
+                         "%.2f, overdensity %.2f, Pk %.2f" % (a.particles, desc, part["ma"],
+                                                             part["overdensity"], part["pk"])}
 
     if rank == 0:
         line = {
@@ -422,16 +518,151 @@ def run_ours(a):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded %s positions, generated on the device)"
                                      % a.positions,
-            "config": workload(a), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "config": workload(a), "roofline": roof, "stages": stages,
+            "cpu_baseline": cpu, "e2e": e2e,
+            "headline": headline, "batched": batched, "served": served,
             "clocks": clk, "gpu_launches": launches,
-            "stages_ms_per_step": stage_ms,
-            "pipeline_algorithmic_bytes": pipe_bytes,
-            "pipeline_frac": pipe_bytes / (ms_step / 1e3) / 1e9 / peak,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+# --------------------------------------------- the metric's headline stream
+def headline_stream(a, P, host, device_value):
+    """The metric's comparison on one request stream: a.headline_requests
+    spectra of the workload (same pinned host positions for every form).
+
+    plain    the drop-in path one request at a time, as the reference's
+             canonical caller (Pk_snapshot.py:66-89): delta = zeros, MA(pos,
+             delta), delta /= mean; delta -= 1 (numpy), Pk(delta) -- host
+             numpy arrays in and out.
+    batched  pylians3_gb300.power_spectra (the grid stays on the device, the
+             upload of one request overlaps the computation of the one
+             before).
+    served   serving.Server (continuous batching: contexts with resident
+             workspaces, HBM-budget admission), all requests submitted at
+             once; and a Poisson stream below saturation for its latency."""
+    import numpy as np
+    from pylians3_gb300.serving import Server
+    K = max(4, a.headline_requests)
+
+    def plain_one():
+        delta = np.zeros((a.dims,) * 3, np.float32)
+        P.MAS_library.MA(host, delta, BOX, a.mas)
+        delta /= (a.particles * 1.0 / a.dims ** 3)
+        delta -= 1.0
+        return P.Pk_library.Pk(delta, BOX, axis=a.axis, MAS=a.mas, threads=1, verbose=False)
+
+    plain_one()
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(K):
+        t1 = time.perf_counter()
+        plain_one()
+        lat.append(time.perf_counter() - t1)
+    t_plain = time.perf_counter() - t0
+    plain = {"value": K / t_plain, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+             "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+             "api": "MAS_library.MA + numpy delta/mean - 1 + Pk_library.Pk, one request at a "
+                    "time, host numpy arrays (Pk_snapshot.py:66-89)"}
+
+    P.power_spectra([host] * 2, a.dims, BOX, a.mas, axis=a.axis)
+    t0 = time.perf_counter()
+    P.power_spectra([host] * K, a.dims, BOX, a.mas, axis=a.axis)
+    t_b = time.perf_counter() - t0
+    batched = {"value": K / t_b, "api": "pylians3_gb300.power_spectra (2 sets in flight)"}
+
+    def serve(slots, arrivals):
+        srv = Server(slots=slots, hbm_budget=150e9)
+        for f in [srv.submit(host, a.dims, BOX, a.mas, axis=a.axis) for _ in range(slots)]:
+            f.result()                     # warm every slot's workspaces
+        srv.done_latencies.clear()
+        t0 = time.perf_counter()
+        futs = []
+        for t_arr in arrivals:
+            now = time.perf_counter() - t0
+            if t_arr > now:
+                time.sleep(t_arr - now)
+            futs.append(srv.submit(host, a.dims, BOX, a.mas, axis=a.axis))
+        for f in futs:
+            f.result()
+        wall = time.perf_counter() - t0
+        lat = srv.latencies()
+        srv.close()
+        return {"value": len(arrivals) / wall, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                "p99_ms": 1e3 * float(np.percentile(lat, 99))}
+
+    served = serve(3, [0.0] * K)
+    served["api"] = "serving.Server, 3 slots, all requests submitted at once"
+    rate = 0.5 * served["value"]
+    rng = np.random.default_rng(99)
+    arr = np.cumsum(rng.exponential(1.0 / rate, size=2 * K))
+    poisson = serve(3, list(arr))
+    poisson["rate_per_s"] = rate
+    poisson["api"] = "serving.Server, 3 slots, Poisson arrivals at half the saturated rate"
+    best = max(batched["value"], served["value"])
+    return {
+        "stream": "%d requests: %d pinned host particles each -> %d^3 %s spectrum, axis %d"
+                  % (K, a.particles, a.dims, a.mas, a.axis),
+        "plain": plain, "batched": batched, "served": served, "served_poisson": poisson,
+        "device_resident": {"value": device_value,
+                            "api": "pyl_pk_particles on device-resident positions (value)"},
+        "ratio_served_batched_vs_plain": best / plain["value"],
+        "ratio_batched_vs_plain": batched["value"] / plain["value"],
+        "ratio_served_vs_plain": served["value"] / plain["value"],
+        "ratio_device_resident_vs_plain": device_value / plain["value"],
+    }
+
+
+def batched_summary(a):
+    """64 uneven realizations (the batched workload), device-resident: one
+    power_spectrum call at a time vs the whole batch as one graph launch vs
+    the server (2 slots).  Tile shapes as tuned and cached, else the
+    built-in rule."""
+    import torch
+    import pylians3_gb300 as P
+    from pylians3_gb300.pipeline import spectra_batch
+    from pylians3_gb300.serving import run_batch
+    reqs = batched_requests(torch)
+    ctx = P.context(0)
+    for r in reqs:
+        P.power_spectrum(**r, ctx=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        P.power_spectrum(**r, ctx=ctx)
+    t_seq = time.perf_counter() - t0
+    spectra_batch(reqs, ctx=ctx)
+    spectra_batch(reqs, ctx=ctx)
+    t0 = time.perf_counter()
+    spectra_batch(reqs, ctx=ctx)
+    t_graph = time.perf_counter() - t0
+    run_batch(reqs, slots=2)
+    _, t_srv = run_batch(reqs, slots=2)
+    out = {"metric": "spectra/s over 64 uneven realizations (dims 128-384, 2^20-2^25 "
+                     "particles, CIC/TSC, half weighted)",
+           "one_at_a_time": len(reqs) / t_seq, "graph_batch": len(reqs) / t_graph,
+           "server_2_slots": len(reqs) / t_srv,
+           "speedup_graph_vs_one_at_a_time": t_seq / t_graph,
+           "particles_total": int(sum(int(r["pos"].shape[0]) for r in reqs))}
+    del reqs
+    torch.cuda.empty_cache()
+    return out
+
+
+def served_summary(a, rates=(100.0, 400.0), seconds=3.0):
+    """Short Poisson streams of the served workload (dims 64-512, any MAS and
+    axis, 1-8 particles per cell): the server (8 slots) against a queue with
+    one slot, spectra/s and p50/p99 latency."""
+    import torch
+    import argparse as _ap
+    b = _ap.Namespace(**vars(a))
+    b.rates, b.seconds, b.slots = list(rates), seconds, 8
+    res = run_served(b, emit=False)
+    torch.cuda.empty_cache()
+    return res
 
 
 # ------------------------------------------------ batched and served forms
@@ -520,7 +751,7 @@ def served_pool(torch, max_ppc=8):
     return {d: synth.uniform(max_ppc * d ** 3, BOX, seed=77 + d) for d in (64, 128, 256, 512)}
 
 
-def run_served(a):
+def run_served(a, emit=True):
     import numpy as np
     import torch
     import pylians3_gb300 as P
@@ -573,7 +804,10 @@ def run_served(a):
             "config": {"dims": "{64,128,256,512} p=(.3,.3,.3,.1)", "particles_per_cell": "U{1..8}",
                        "mas": "U{NGP,CIC,TSC,PCS}", "axis": "U{0,1,2}",
                        "positions": "device-resident uniform pools", "hbm_budget_gb": 150}}
-    print(json.dumps(line), flush=True)
+    del pool
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 # --------------------------------------------------------------- precision

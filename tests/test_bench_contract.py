@@ -1,6 +1,6 @@
-"""The JSON line of bench.py's reference arm (the oracle port timed on the
-host cores) on a tiny workload: the keys and types the benchmark contract
-asks for.  CPU only."""
+"""The JSON line of bench.py's reference arm (the reference's own CPU code,
+compiled here, or the oracle port) on a tiny workload: the keys and types
+the benchmark contract asks for, and that full spectra are timed.  CPU only."""
 import json
 import os
 import subprocess
@@ -11,8 +11,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_line():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--dims", "32", "--particles", "32768", "--steps", "1", "--warmup", "0",
-                        "--cpu-sample", "1"], capture_output=True, text=True, cwd=ROOT, timeout=600)
+                        "--dims", "32", "--particles", "32768", "--steps", "2", "--warmup", "0"],
+                       capture_output=True, text=True, cwd=ROOT, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
@@ -21,12 +21,13 @@ def test_reference_arm_line():
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
               "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config"):
         assert k in d, k
-    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 2
+    assert abs(d["ms_per_step"] - 1e3 / d["value"]) < 1e-6 * d["ms_per_step"]
     assert d["config"]["workload"].startswith("32^3 grid, 32768 uniform particles")
     assert "smaller than L2" in d["config"]["l2"]
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
-    assert cb["unit"] == d["unit"] and cb["sample"]
+    assert cb["unit"] == d["unit"] and cb["sample"].startswith("2 full spectra (all 32768")
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
