@@ -5,8 +5,10 @@
   the fused particles -> spectrum path (what bench.py times) and the drop-in
   MA -> delta/mean - 1 -> Pk sequence on the device, against the oracle on
   the same seeded positions.  The oracle deposit is the reference's OpenMP
-  one (MAS_c.c:8-266 restated; float32 atomics on all cores), its overdensity
-  and its Pk (Pk_library.pyx:311-418; mode-loop rows on all cores).  Mode
+  one (MAS_c.c:8-266 restated; float32 atomics on all cores; its serial MA,
+  MAS_library.pyx:123-166 / 369-404, is a second summation order for the
+  gate), its overdensity and its Pk (Pk_library.pyx:311-418; mode-loop rows
+  on all cores).  Mode
   counts are compared exactly, k3D to float64 rounding, and P_ell per bin
   against the gate of tests/gates.py: |dP_ell| / |P0| <= 1e-4, or a small
   multiple of the reference's own float32-vs-float64 error where that is
@@ -19,7 +21,7 @@ import os
 import numpy as np
 import pytest
 
-from gates import TOL_PK, check, per_bin_err
+from gates import TOL_PK, check, float32_gate, per_bin_err
 
 pytestmark = pytest.mark.gpu
 
@@ -54,20 +56,26 @@ def test_mode_counts_bit_exact(gpu, oracle, dims, axis):
     np.testing.assert_allclose(r.k1D, m["k1D"] * kF, rtol=1e-12)
 
 
-def _oracle_pair(oracle, pos_np, dims, MAS, axis):
+def _oracle_spectra(oracle, pos_np, dims, MAS, axis):
     """Oracle spectra of the same positions: float32 (the reference's
-    arithmetic) and float64 (its precision restatement)."""
-    g = np.zeros((dims,) * 3, np.float32)
-    oracle.deposit_omp(MAS, pos_np, g, BOX, threads=0)
-    g /= np.mean(g, dtype=np.float64)
-    g -= 1.0
-    ref32 = oracle.Pk(g, BOX, axis=axis, MAS=MAS, threads=NCPU, bin_threads=0)
-    del g
+    arithmetic) with the OpenMP deposit (MAS_c.c) and with the serial one
+    (MA), and float64 (the precision restatement)."""
+    refs = []
+    for dep in ("omp", "serial"):
+        g = np.zeros((dims,) * 3, np.float32)
+        if dep == "omp":
+            oracle.deposit_omp(MAS, pos_np, g, BOX, threads=0)
+        else:
+            oracle.MA(pos_np, g, BOX, MAS)
+        g /= np.mean(g, dtype=np.float64)
+        g -= 1.0
+        refs.append(oracle.Pk(g, BOX, axis=axis, MAS=MAS, threads=NCPU, bin_threads=0))
+        del g
     g64 = oracle.MA_f64(pos_np, dims, BOX, MAS, threads=0)
     g64 /= g64.mean()
     g64 -= 1.0
     ref64 = oracle.Pk_f64(g64, BOX, axis=axis, MAS=MAS, threads=NCPU, bin_threads=0)
-    return ref32, ref64
+    return refs, ref64
 
 
 def _compare(gpu, oracle, pos, dims, MAS, axis, label):
@@ -81,18 +89,23 @@ def _compare(gpu, oracle, pos, dims, MAS, axis, label):
     del grid
     pos_np = pos.cpu().numpy()
     torch.cuda.empty_cache()
-    ref32, ref64 = _oracle_pair(oracle, pos_np, dims, MAS, axis)
+    refs, ref64 = _oracle_spectra(oracle, pos_np, dims, MAS, axis)
+    ref32 = refs[0]
     for name, r in (("fused", fused), ("drop-in", dropin)):
         assert np.array_equal(r.Nmodes3D, ref32.Nmodes3D), name
         np.testing.assert_allclose(r.k3D, ref32.k3D, rtol=1e-12)
         err = per_bin_err(r.Pk, ref32.Pk)
         mid = dims // 2
-        e_ref = per_bin_err(ref32.Pk, ref64.Pk)
-        print("\n%s %s: max err <= k_N %.2e, all bins %.2e (bins > 1e-4: %d, reference "
-              "float32 vs float64: <= k_N %.2e, all %.2e, bins > 1e-4: %d)"
-              % (label, name, err[:mid].max(), err.max(), int((err > TOL_PK).sum()),
-                 e_ref[:mid].max(), e_ref.max(), int((e_ref > TOL_PK).sum())))
-        check(r.Pk, ref32.Pk, ref64.Pk, "%s %s" % (label, name))
+        e_ref = np.max([per_bin_err(q.Pk, ref64.Pk) for q in refs], axis=0)
+        gate = float32_gate([q.Pk for q in refs], ref64.Pk, ref32.Nmodes3D)
+        print("\n%s %s: max err <= k_N %.2e, all bins %.2e (bins > 1e-4: %d; last bin %.2e, "
+              "gate %.2e, Nmodes %d); reference float32 vs float64: <= k_N %.2e, all %.2e, "
+              "bins > 1e-4: %d"
+              % (label, name, err[:mid].max(), err.max(), int((err > TOL_PK).sum()), err[-1],
+                 gate[-1], int(ref32.Nmodes3D[-1]), e_ref[:mid].max(), e_ref.max(),
+                 int((e_ref > TOL_PK).sum())))
+        check(r.Pk, ref32.Pk, ref64.Pk, ref32.Nmodes3D, "%s %s" % (label, name),
+              refs32=[q.Pk for q in refs])
         # up to the Nyquist wavenumber the flat tolerance holds everywhere
         assert err[:mid].max() <= TOL_PK
 

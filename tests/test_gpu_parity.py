@@ -217,7 +217,7 @@ def test_pk_3x2k_lengths_vs_oracle(gpu, oracle, dims, MAS, axis):
     g64 /= g64.mean()
     g64 -= 1.0
     ref64 = oracle.Pk_f64(g64, BOX, axis=axis, MAS=MAS, threads=8)
-    check(s.Pk, ref.Pk, ref64.Pk, "fused %d^3 %s" % (dims, MAS))
+    check(s.Pk, ref.Pk, ref64.Pk, ref.Nmodes3D, "fused %d^3 %s" % (dims, MAS))
 
 
 # ------------------------------------------------------------------ FFTs
