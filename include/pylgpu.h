@@ -92,6 +92,14 @@ int pyl_ctx_workspace_bytes(const pyl_ctx *ctx, size_t *bytes);
 int pyl_ctx_trim(pyl_ctx *ctx);
 /* Number of kernel launches this context has issued (for accounting).     */
 int pyl_ctx_launch_count(const pyl_ctx *ctx, int64_t *count);
+/* The tile sort of the last collected pyl_pk_particles request (no
+ * reference counterpart; for tests and tuning): *count_free = 1 when it ran
+ * without a counting pass (fixed slots sized from the previous request of
+ * the same dims, scheme and weighting), 0 for the exact counting sort, -1
+ * when the deposit was not sorted; *spilled = particles that overflowed
+ * their slots and were added by a global-atomic deposit instead (the next
+ * request of that kind then takes the exact sort).                         */
+int pyl_ctx_last_sort(const pyl_ctx *ctx, int *count_free, unsigned *spilled);
 /* Stage timing with CUDA events on the context stream (off by default).
  * pyl_ctx_stage_times waits for recorded events, writes the accumulated
  * milliseconds and launch counts of the first n stages (names from

@@ -40,7 +40,7 @@ PYL_PK_1D, PYL_PK_2D, PYL_PK_PHASE, PYL_PK_ALL = 0x01, 0x02, 0x04, 0x07
 EXPORTS = (
     "pyl_ctx_create", "pyl_ctx_destroy", "pyl_ctx_set_stream", "pyl_ctx_get_stream",
     "pyl_synchronize", "pyl_last_error", "pyl_ctx_workspace_bytes", "pyl_ctx_trim",
-    "pyl_ctx_launch_count", "pyl_host_alloc", "pyl_host_free", "pyl_ma", "pyl_ma_f64",
+    "pyl_ctx_launch_count", "pyl_ctx_last_sort", "pyl_host_alloc", "pyl_host_free", "pyl_ma", "pyl_ma_f64",
     "pyl_fft_r2c", "pyl_fft_c2r", "pyl_pk_sizes", "pyl_pk", "pyl_pk_particles",
     "pyl_ctx_set_timing", "pyl_ctx_stage_times", "pyl_stage_name", "pyl_pk_noalloc",
     "pyl_pk_particles_enqueue", "pyl_pk_query", "pyl_pk_collect",
@@ -102,6 +102,7 @@ def load():
             "pyl_ctx_workspace_bytes": [vp, ctypes.POINTER(sz)],
             "pyl_ctx_trim": [vp],
             "pyl_ctx_launch_count": [vp, ctypes.POINTER(i64)],
+            "pyl_ctx_last_sort": [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_uint)],
             "pyl_ctx_set_timing": [vp, i32],
             "pyl_ctx_stage_times": [vp, ctypes.POINTER(f64), ctypes.POINTER(i64), i32, i32],
             "pyl_host_alloc": [ctypes.POINTER(vp), sz],
@@ -177,6 +178,14 @@ class Context:
         v = ctypes.c_int64()
         self.check(self.lib.pyl_ctx_launch_count(self.ptr, ctypes.byref(v)))
         return v.value
+
+    def last_sort(self):
+        """(count_free, spilled) of the last collected particles request:
+        count_free 1 = the sort without a counting pass, 0 = the exact
+        counting sort, -1 = no sorted deposit."""
+        cf, sp = ctypes.c_int(), ctypes.c_uint()
+        self.check(self.lib.pyl_ctx_last_sort(self.ptr, ctypes.byref(cf), ctypes.byref(sp)))
+        return cf.value, sp.value
 
     def set_timing(self, on: bool):
         self.check(self.lib.pyl_ctx_set_timing(self.ptr, 1 if on else 0))

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <tuple>
 #include <string>
 #include <utility>
 #include <vector>
@@ -85,6 +86,26 @@ struct pyl_ctx {
     double stage_ms[ST_NSTAGES] = {};
     int64_t stage_n[ST_NSTAGES] = {};
 
+    // Count-free ("capacity") tile sort of the fused particles path: per
+    // (dims, scheme, weighted), what the last request showed.  After an
+    // exact sort, the largest tile and coarse-bucket counts relative to
+    // their means (phiT, phiC) size fixed slots for the next request, which
+    // then needs no counting pass; a request whose slots overflowed (its
+    // particles went to the spill list) sends the next one back to the
+    // exact sort.  mode: the sort the exact pass chose (frontier/two-pass).
+    struct SortPlan { bool cap = false; float phiT = 0.f, phiC = 0.f; int mode = -1; };
+    std::map<std::tuple<int, int, int>, SortPlan> sort_plans;
+    SortPlan *sort_hint = nullptr;     // set by the particles path around deposit()
+    struct SortUsed {
+        bool valid = false, cap = false;
+        int ntiles = 0, F = 0;
+        long long n = 0;
+        SortPlan *plan = nullptr;
+    } sort_used;                       // what the last sorted deposit did
+    unsigned *d_sort_info = nullptr;   // its 4 info words on the device
+    int last_sort_cap = -1;            // the last collected request's sort (pyl_ctx_last_sort)
+    unsigned last_spilled = 0;
+
     // The request issued by pyl_pk_particles_enqueue and not yet collected:
     // its raw sums are copied to `pinned` and `done` is recorded after them.
     struct Request {
@@ -93,6 +114,7 @@ struct pyl_ctx {
         double BoxSize = 0.0;
         const pyl::ModeTables *T = nullptr;
         pyl::AccLayout L;
+        SortUsed sort;        // its sorted deposit; its info words follow the sums
     } req;
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -100,6 +122,14 @@ struct pyl_ctx {
 
     struct Buf { void *p = nullptr; size_t bytes = 0; };
     std::map<std::string, Buf> ws;                       // named workspaces
+
+    // A second stream for work that can run beside the sort: the grid of
+    // the fused particles path is zeroed there (created on first use).
+    // grid_pending: that zeroing is issued and the context stream has not
+    // yet waited for it (wait_grid).
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool grid_pending = false;
 
     // Status word the kernels set when a bounded wait gives up (bits of
     // kStatusWaitTimeout, async_copy.cuh); read and cleared by status_check.
@@ -153,6 +183,13 @@ const float *window_table(pyl_ctx *ctx, int dims, int mas, int *status);
 // ---------------------------------------------------------------- launchers
 // deposit.cu: grid += deposit of n particles (grid extent dims^2 * dz where
 // dz = dims for coord 3 and 1 for coord 2).  All pointers are device pointers.
+// Zeroes `bytes` at p on the context's side stream after the work already
+// on the context stream, so that it overlaps what the context stream does
+// next; wait_grid makes the context stream wait for it (a no-op when nothing
+// is pending).  Every kernel that touches the grid calls wait_grid first.
+int zero_beside(pyl_ctx *ctx, void *p, size_t bytes);
+int wait_grid(pyl_ctx *ctx);
+
 int deposit(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,
             float *grid, int dims, float BoxSize, int mas, int flags);
 int deposit_f64(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const float *W,

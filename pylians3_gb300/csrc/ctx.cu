@@ -72,6 +72,27 @@ void *ws_get(pyl_ctx *ctx, const char *name, size_t bytes, int *status) {
     return b.p;
 }
 
+int zero_beside(pyl_ctx *ctx, void *p, size_t bytes) {
+    if (!ctx->side) {
+        PYL_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        PYL_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        PYL_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    }
+    PYL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
+    PYL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    PYL_CUDA(ctx, cudaMemsetAsync(p, 0, bytes, ctx->side));
+    PYL_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+    ctx->grid_pending = true;
+    return PYL_OK;
+}
+
+int wait_grid(pyl_ctx *ctx) {
+    if (!ctx->grid_pending) return PYL_OK;
+    ctx->grid_pending = false;
+    PYL_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+    return PYL_OK;
+}
+
 void stage_mark(pyl_ctx *ctx, int stage, bool begin) {
     if (!ctx->timing) return;
     cudaEvent_t ev;
@@ -310,6 +331,7 @@ int pyl_ctx_create(pyl_ctx **out, int device, void *stream) {
 }
 
 static void release_all(pyl_ctx *ctx) {
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     cudaStreamSynchronize(ctx->stream);
     for (auto &kv : ctx->ws) if (kv.second.p) cudaFree(kv.second.p);
     ctx->ws.clear();
@@ -329,6 +351,9 @@ int pyl_ctx_destroy(pyl_ctx *ctx) {
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
     if (ctx->batch_pinned) cudaFreeHost(ctx->batch_pinned);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PYL_OK;
@@ -404,6 +429,13 @@ const char *pyl_stage_name(int stage) {
                                             "fft_y", "fft_x", "pk_x", "d2h", "tile_count",
                                             "mass"};
     return (stage >= 0 && stage < ST_NSTAGES) ? names[stage] : "";
+}
+
+int pyl_ctx_last_sort(const pyl_ctx *ctx, int *count_free, unsigned *spilled) {
+    if (!ctx || !count_free || !spilled) return PYL_ERR_ARG;
+    *count_free = ctx->last_sort_cap;
+    *spilled = ctx->last_spilled;
+    return PYL_OK;
 }
 
 int pyl_ctx_launch_count(const pyl_ctx *ctx, int64_t *count) {
@@ -731,12 +763,13 @@ int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, 
     const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
     float *grid = (float *)ws_get(ctx, "pk_grid", rb, &st);
     if (!grid) return st;
-    {
-        StageScope s(ctx, ST_ZERO);
-        PYL_CUDA(ctx, cudaMemsetAsync(grid, 0, rb, ctx->stream));
-    }
-    if ((st = deposit(ctx, dpos, n, 3, dW, grid, dims, r.BoxSize, r.mas_deposit, flags)))
-        return st;
+    // the grid is zeroed beside the sort (which is bound by shared memory,
+    // not DRAM); the deposit waits for it
+    if ((st = zero_beside(ctx, grid, rb))) return st;
+    st = deposit(ctx, dpos, n, 3, dW, grid, dims, r.BoxSize, r.mas_deposit, flags);
+    const int st2 = wait_grid(ctx);
+    if (st) return st;
+    if (st2) return st2;
     void *acc = nullptr;
     AccLayout L;
     const MassInfo mi{dW, n};
@@ -745,7 +778,30 @@ int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, 
     const size_t nb = L.sums() + sizeof(float2) + sizeof(double);
     StageScope s(ctx, ST_D2H);
     PYL_CUDA(ctx, cudaMemcpyAsync(dst, acc, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->sort_hint && ctx->sort_used.valid && ctx->d_sort_info)
+        PYL_CUDA(ctx, cudaMemcpyAsync((char *)dst + nb, ctx->d_sort_info, 4 * sizeof(unsigned),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
     return PYL_OK;
+}
+
+// What the finished request's sorted deposit showed (its info words, copied
+// after the sums) decides the sort of the next request of its kind: after
+// an exact sort, slots sized from the largest tile and bucket counts (with a
+// margin) unless the input is clustered; after a count-free sort whose slots
+// overflowed, the exact sort again.
+void learn_sort(const pyl_ctx::SortUsed &u, const unsigned *info) {
+    if (!u.valid || !u.plan) return;
+    pyl_ctx::SortPlan &p = *u.plan;
+    if (u.cap) {
+        if (info[3] != 0) p.cap = false;
+        return;
+    }
+    const double mean_t = (double)u.n / u.ntiles;
+    const double phiT = info[0] / mean_t, phiC = info[1] / (mean_t * u.F);
+    p.phiT = (float)std::max(1.05, 1.1 * phiT);
+    p.phiC = (float)std::max(1.03, 1.05 * phiC);
+    p.mode = (int)info[2];
+    p.cap = p.phiT <= 2.0f && p.phiC <= 2.0f && mean_t >= 64.0;
 }
 
 // Spectrum of a request from the raw sums, k = 0 mode and mass at `src`.
@@ -839,7 +895,7 @@ int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const fl
     const ModeTables *T = mode_tables(ctx, dims, axis, &st);
     if (!T) return st;
     const AccLayout L = acc_layout(*T);
-    const size_t nb = L.sums() + sizeof(float2) + sizeof(double);
+    const size_t nb = L.sums() + sizeof(float2) + sizeof(double) + 4 * sizeof(unsigned);
     if (ctx->pinned_bytes < nb) {
         if (ctx->pinned) {
             PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -851,8 +907,12 @@ int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const fl
         ctx->pinned_bytes = nb;
     }
     if (!ctx->done) PYL_CUDA(ctx, cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming));
-    if ((st = issue_particles(ctx, r, *T, flags, ctx->pinned))) return st;
+    ctx->sort_hint = &ctx->sort_plans[std::make_tuple(dims, mas_deposit, W ? 1 : 0)];
+    st = issue_particles(ctx, r, *T, flags, ctx->pinned);
+    ctx->sort_hint = nullptr;
+    if (st) return st;
     PYL_CUDA(ctx, cudaEventRecord(ctx->done, ctx->stream));
+    ctx->req.sort = ctx->sort_used;
     ctx->req.active = true;
     ctx->req.dims = dims;
     ctx->req.axis = axis;
@@ -905,6 +965,11 @@ int pyl_pk_collect(pyl_ctx *ctx, pyl_pk_out *out, int timeout_ms) {
     ctx->req.active = false;
     if ((st = status_check(ctx))) return st;
     const pyl_ctx::Request &R = ctx->req;
+    const unsigned *info = (const unsigned *)((const char *)ctx->pinned + R.L.sums() +
+                                              sizeof(float2) + sizeof(double));
+    learn_sort(R.sort, info);
+    ctx->last_sort_cap = R.sort.valid ? (R.sort.cap ? 1 : 0) : -1;
+    ctx->last_spilled = (R.sort.valid && R.sort.cap) ? info[3] : 0u;
     return finalize_particles(ctx, *R.T, R.L, ctx->pinned, R.dims, R.BoxSize, R.what, out);
 }
 

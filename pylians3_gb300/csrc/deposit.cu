@@ -23,6 +23,7 @@
 // index 0 and weight 1 for every tap, so a particle is deposited 2/3/4 times
 // onto the same plane for CIC/TSC/PCS (and renormalised by the caller).
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <type_traits>
 
@@ -37,14 +38,17 @@ constexpr int kThreads = 256;
 
 // ------------------------------------------------------------ unsorted path
 // COMP: compensated float adds, errors into lo (same layout as the grid).
+// n_dev (may be null): the particle count is min(n, *n_dev), read on the
+// device (the spill list of the count-free sort).
 template <int MAS, bool HAS_W, typename G, bool COMP>
 __global__ void __launch_bounds__(kThreads)
 k_deposit_atomic(const float *__restrict__ pos, long long n, int coord,
                  const float *__restrict__ W, G *__restrict__ grid, int dims,
-                 float inv, float *__restrict__ lo) {
+                 float inv, float *__restrict__ lo, const unsigned *__restrict__ n_dev) {
     static_assert(!COMP || sizeof(G) == sizeof(float), "compensation is for float32 grids");
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
+    if (n_dev && (long long)*n_dev < n) n = (long long)*n_dev;
     const long long sy = coord == 3 ? dims : 1;
     const long long sx = sy * dims;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -133,10 +137,12 @@ int launch_atomic(pyl_ctx *ctx, const float *pos, long long n, int coord, const 
     long long blocks = (n + kThreads - 1) / kThreads;
     if (blocks > 152LL * 64) blocks = 152LL * 64;
     if (blocks < 1) blocks = 1;
+    int st = wait_grid(ctx);
+    if (st) return st;
     StageScope s(ctx, ST_DEPOSIT);
     auto go = [&](auto kernel) {
         kernel<<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(pos, n, coord, W, grid, dims, inv,
-                                                               lo);
+                                                               lo, nullptr);
     };
     if constexpr (sizeof(G) == sizeof(float)) {
         if (lo) {
@@ -443,20 +449,33 @@ k_tile_count4(const float4 *__restrict__ pos4, const float *__restrict__ pos, lo
 // when a warp's 32 particles span at most 8 tiles on average).
 constexpr int kSortFrontier = 0, kSortTwoPass = 1;
 
+// info (4 words, zeroed): [0] the largest tile count, [1] the largest coarse
+// bucket count, [2] the sort chosen -- what the count-free sort of the next
+// request sizes its slots from.
 __global__ void k_sort_setup(const unsigned *__restrict__ start, int ntiles, int F, int ncoarse,
                              unsigned *__restrict__ fine_cur, unsigned *__restrict__ coarse_cur,
                              unsigned *__restrict__ nchunk, long long n,
                              const unsigned *__restrict__ distinct, int forced,
-                             unsigned *__restrict__ mode) {
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        *mode = forced >= 0 ? (unsigned)forced
-                            : ((long long)*distinct * 4 <= n ? kSortFrontier : kSortTwoPass);
+                             unsigned *__restrict__ mode, unsigned *__restrict__ info) {
+    const unsigned m = forced >= 0 ? (unsigned)forced
+                                   : ((long long)*distinct * 4 <= n ? kSortFrontier : kSortTwoPass);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *mode = m;
+        info[2] = m;
+    }
+    unsigned mt = 0, mc = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
         fine_cur[t] = start[t];
         const unsigned cnt = start[t + 1] - start[t];
         nchunk[t] = (cnt + kItemCap - 1) / kItemCap;
-        if (t % F == 0) coarse_cur[t / F] = start[t];
+        mt = max(mt, cnt);
+        if (t % F == 0) {
+            coarse_cur[t / F] = start[t];
+            mc = max(mc, start[min(t + F, ntiles)] - start[t]);
+        }
     }
+    if (mt) atomicMax(&info[0], mt);
+    if (mc) atomicMax(&info[1], mc);
 }
 
 __global__ void k_items(const unsigned *__restrict__ nchunk_ex, const unsigned *__restrict__ start,
@@ -638,18 +657,240 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
     }
 }
 
+// Count-free partition pass into fixed-capacity slots (the "capacity" sort,
+// used when the previous request of the same kind showed the occupancy of
+// tiles and coarse buckets; no counting pass, no scan).
+//   FINE = false: keys are coarse buckets of the input particles; bucket c
+//     owns dst[c * cap, (c + 1) * cap).
+//   FINE = true: the input is the coarse pass's output -- bucket c's
+//     particles are src[c * cap_in, c * cap_in + min(count_in[c], cap_in)) --
+//     and the keys are the bucket's tiles; tile t owns dst[t * cap, ...).
+// A key's cursor counts all its particles; the part of a run beyond the
+// key's capacity goes to the spill list (spill[*spill_n ...]), which a
+// global-atomic deposit adds to the grid.  Chunks never straddle buckets.
+// Otherwise as k_partition: persistent CTAs, the next chunk fetched by a
+// bulk copy while the current one is partitioned (bounded mbarrier waits),
+// a shared counting sort, each key's run written contiguously.
+template <int MAS, bool HAS_W, bool FINE>
+__global__ void __launch_bounds__(kPartThreads, PYL_PART_MINB)
+k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
+                const unsigned *__restrict__ count_in, unsigned cap_in, long long n,
+                float *__restrict__ dst, float *__restrict__ dstw, unsigned cap,
+                unsigned *__restrict__ cursor, float inv, TileGeom g, int bulk,
+                float *__restrict__ spill, float *__restrict__ spillw,
+                unsigned *__restrict__ spill_n, unsigned *__restrict__ status) {
+    extern __shared__ __align__(16) float sm[];
+    constexpr int WS = HAS_W ? KP : 0;
+    float *sp2 = sm + 6 * KP + 2 * WS;                   // 3*KP in key order
+    float *sw2 = sp2 + 3 * KP;
+    unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + WS);
+    unsigned short *skey2 = skey + KP;
+    unsigned *hist = reinterpret_cast<unsigned *>(skey2 + KP);   // kMaxKeys each
+    unsigned *gdiff = hist + kMaxKeys;   // slot of key-ordered element e: gdiff[key] + e
+    unsigned *glim = gdiff + kMaxKeys;   // elements e < glim[key] fit their slots
+    unsigned *gsp = glim + kMaxKeys;     // spill index of the others: gsp[key] + e
+    unsigned *cpre = gsp + kMaxKeys;                     // kMaxKeys + 1 (fine pass)
+    __shared__ unsigned s_warp[32];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ long long s_r0[2];        // fine pass: the next chunk's mapping, by
+    __shared__ int s_ck[2][3];           // buffer (written by thread 0)
+
+    // chunks: the input in KP pieces (coarse), or each bucket's particles in
+    // KP pieces (fine; cpre = exclusive prefix of the chunks per bucket)
+    long long nchunks;
+    if (FINE) {
+        const int c = threadIdx.x;
+        const unsigned cnt = c < g.ncoarse ? min(count_in[c], cap_in) : 0u;
+        unsigned tot = 0;
+        const unsigned ex = block_exclusive_scan((cnt + KP - 1) / KP, s_warp, &tot);
+        if (c < g.ncoarse) cpre[c] = ex;
+        if (c == 0) cpre[g.ncoarse] = tot;
+        __syncthreads();
+        nchunks = tot;
+    } else {
+        nchunks = (n + KP - 1) / KP;
+    }
+    long long c = blockIdx.x;
+    if (c >= nchunks) return;
+    // chunk v -> first particle, count, key base and key count
+    auto map_chunk = [&](long long v, long long &r0, int &cnt, int &keybase, int &nkeys) {
+        if (FINE) {
+            int lo = 0, hi = g.ncoarse - 1;            // last bucket b with cpre[b] <= v
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if ((long long)cpre[mid] <= v) lo = mid;
+                else hi = mid - 1;
+            }
+            const long long k = v - cpre[lo];
+            const long long m = min(count_in[lo], cap_in);
+            r0 = (long long)lo * cap_in + k * KP;
+            cnt = (int)min((long long)KP, m - k * KP);
+            keybase = lo * g.F;
+            nkeys = min(g.F, g.ntiles - keybase);
+        } else {
+            r0 = v * KP;
+            cnt = (int)min((long long)KP, n - r0);
+            keybase = 0;
+            nkeys = g.ncoarse;
+        }
+    };
+    auto issue = [&](long long r0, int b) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&s_bar[b], (12u + (HAS_W ? 4u : 0u)) * KP);
+        bulk_copy_g2s(sm + 3 * KP * b, src + 3 * r0, 12u * KP, &s_bar[b]);
+        if (HAS_W) bulk_copy_g2s(sm + 6 * KP + WS * b, srcw + r0, 4u * KP, &s_bar[b]);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    unsigned parity = 0u, pend = 0u;
+    long long r0;
+    int cnt, keybase, nkeys;
+    map_chunk(c, r0, cnt, keybase, nkeys);
+    if (bulk && cnt == KP) {
+        if (threadIdx.x == 0) issue(r0, 0);
+        pend |= 1u;
+    }
+    int b = 0;
+    for (; c < nchunks; c += gridDim.x, b ^= 1) {
+        const long long cn = c + gridDim.x;
+        long long nr0 = 0;
+        int ncnt = 0, nkb = 0, nnk = 0;
+        if (cn < nchunks) {
+            if (FINE) {
+                // one thread maps the next chunk (a binary search over the
+                // buckets) and passes it on through shared memory, read
+                // after this chunk's last barrier
+                if (threadIdx.x == 0) {
+                    map_chunk(cn, nr0, ncnt, nkb, nnk);
+                    s_r0[b ^ 1] = nr0;
+                    s_ck[b ^ 1][0] = ncnt;
+                    s_ck[b ^ 1][1] = nkb;
+                    s_ck[b ^ 1][2] = nnk;
+                    if (bulk && ncnt == KP) {
+                        issue(nr0, b ^ 1);
+                        pend |= 2u >> b;   // the others learn of it after the barrier
+                    }
+                }
+            } else {
+                map_chunk(cn, nr0, ncnt, nkb, nnk);
+                if (bulk && ncnt == KP) {
+                    if (threadIdx.x == 0) issue(nr0, b ^ 1);
+                    pend |= 2u >> b;
+                }
+            }
+        }
+        float *sp = sm + 3 * KP * b;
+        float *sw = sm + 6 * KP + WS * b;
+        if (pend & (1u << b)) {
+            const unsigned ph = (parity >> b) & 1u;
+            const bool ok = mbar_wait_parity(&s_bar[b], ph);
+            parity ^= 1u << b;
+            pend &= ~(1u << b);
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) atomicOr(status, kStatusWaitTimeout);
+                mbar_wait_parity(&s_bar[b], ph);
+                if (pend) mbar_wait_parity(&s_bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+                return;
+            }
+        } else {
+            for (int j = threadIdx.x; j < 3 * cnt; j += blockDim.x) sp[j] = __ldcs(src + 3 * r0 + j);
+            if (HAS_W)
+                for (int j = threadIdx.x; j < cnt; j += blockDim.x) sw[j] = __ldcs(srcw + r0 + j);
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < nkeys; k += blockDim.x) hist[k] = 0u;
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const float *q = sp + 3 * i;
+            const int t = tile_of<MAS>(q[0], q[1], q[2], inv, g);
+            const int key = FINE ? t - keybase : t / g.F;
+            skey[i] = (unsigned short)key;
+            atomicAdd(&hist[key], 1u);
+        }
+        __syncthreads();
+        const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
+        unsigned my_base = 0u, room = 0u, sb = 0u;
+        if (hv) {
+            my_base = atomicAdd(&cursor[keybase + threadIdx.x], hv);
+            room = my_base >= cap ? 0u : min(hv, cap - my_base);
+            if (hv > room) sb = atomicAdd(spill_n, hv - room);
+        }
+        const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
+        if (threadIdx.x < nkeys) hist[threadIdx.x] = ex;   // running cursor of the counting sort
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const int key = skey[i];
+            const unsigned r = atomicAdd(&hist[key], 1u);
+            const float *q = sp + 3 * i;
+            sp2[3 * r] = q[0];
+            sp2[3 * r + 1] = q[1];
+            sp2[3 * r + 2] = q[2];
+            if (HAS_W) sw2[r] = sw[i];
+            skey2[r] = (unsigned short)key;
+        }
+        if (threadIdx.x < nkeys) {
+            // unsigned arithmetic modulo 2^32: every slot and spill index is
+            // below 2^32 (the host checks the slot arrays' sizes)
+            gdiff[threadIdx.x] = (unsigned)(keybase + threadIdx.x) * cap + my_base - ex;
+            glim[threadIdx.x] = ex + room;
+            gsp[threadIdx.x] = sb - (ex + room);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const int key = skey2[e];
+            const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
+            if ((unsigned)e < glim[key]) {
+                const size_t d = gdiff[key] + (unsigned)e;
+                dst[3 * d] = x;
+                dst[3 * d + 1] = y;
+                dst[3 * d + 2] = z;
+                if (HAS_W) dstw[d] = sw2[e];
+            } else {
+                const size_t d = gsp[key] + (unsigned)e;
+                spill[3 * d] = x;
+                spill[3 * d + 1] = y;
+                spill[3 * d + 2] = z;
+                if (HAS_W) spillw[d] = sw2[e];
+            }
+        }
+        __syncthreads();
+        if (FINE && cn < nchunks) {
+            // thread 0's mapping of the next chunk; a copy is in flight for
+            // it when it is a whole chunk
+            nr0 = s_r0[b ^ 1];
+            ncnt = s_ck[b ^ 1][0];
+            nkb = s_ck[b ^ 1][1];
+            nnk = s_ck[b ^ 1][2];
+            if (bulk && ncnt == KP) pend |= 2u >> b;
+        }
+        r0 = nr0;
+        cnt = ncnt;
+        keybase = nkb;
+        nkeys = nnk;
+    }
+}
+
 // Single-pass alternative to the two partition passes: every particle takes
 // the next slot of its tile with one atomic on the tile's global cursor
 // (lanes of a warp that share a tile take one atomic for all of them).
 // All writes of a tile happen at its advancing frontier, so the partially
 // written sectors stay in L2 until they are complete.
+// cap > 0 (the count-free sort): tile t owns dst[t * cap, (t + 1) * cap),
+// cursor[t] counts its particles from 0, and a particle beyond the capacity
+// goes to the spill list; mode is then not read.
 template <int MAS, bool HAS_W>
 __global__ void __launch_bounds__(256)
 k_scatter_frontier(const float *__restrict__ src, const float *__restrict__ srcw, long long n,
                    float inv, TileGeom g, unsigned *__restrict__ cursor,
                    float *__restrict__ dst, float *__restrict__ dstw,
-                   const unsigned *__restrict__ mode) {
-    if (*mode != kSortFrontier) return;   // the whole grid takes the same branch
+                   const unsigned *__restrict__ mode, unsigned cap,
+                   float *__restrict__ spill, float *__restrict__ spillw,
+                   unsigned *__restrict__ spill_n) {
+    if (!cap && *mode != kSortFrontier) return;   // the whole grid takes the same branch
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     for (long long b = (long long)blockIdx.x * blockDim.x; b < n;
@@ -666,11 +907,20 @@ k_scatter_frontier(const float *__restrict__ src, const float *__restrict__ srcw
         unsigned base = 0;
         if (lane == leader) base = atomicAdd(&cursor[t], (unsigned)__popc(peers));
         base = __shfl_sync(peers, base, leader);
-        const size_t slot = (size_t)base + __popc(peers & lt);
-        dst[3 * slot] = x;
-        dst[3 * slot + 1] = y;
-        dst[3 * slot + 2] = z;
-        if (HAS_W) dstw[slot] = __ldcs(srcw + i);
+        const unsigned r = base + __popc(peers & lt);
+        if (!cap || r < cap) {
+            const size_t slot = cap ? (size_t)t * cap + r : (size_t)r;
+            dst[3 * slot] = x;
+            dst[3 * slot + 1] = y;
+            dst[3 * slot + 2] = z;
+            if (HAS_W) dstw[slot] = __ldcs(srcw + i);
+        } else {
+            const size_t slot = atomicAdd(spill_n, 1u);
+            spill[3 * slot] = x;
+            spill[3 * slot + 1] = y;
+            spill[3 * slot + 2] = z;
+            if (HAS_W) spillw[slot] = __ldcs(srcw + i);
+        }
     }
 }
 
@@ -771,12 +1021,17 @@ __device__ __forceinline__ bool fixed_exponent(float m, int &e) {
     return true;
 }
 
+// Work items: items[0 .. *nitems) over the exact sort's tile starts, or
+// with cap_count (the count-free sort) the fixed grid of ntiles * ipt items
+// (tile it / ipt, chunk it % ipt) over the tile slots of capT particles,
+// tile t holding min(cap_count[t], capT) of them.
 template <int MAS, bool HAS_W, int ACC>
 __global__ void __launch_bounds__(512)
 k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                const unsigned *__restrict__ start, const uint2 *__restrict__ items,
                const unsigned *__restrict__ nitems, float inv, TileGeom g,
-               float *__restrict__ grid, int vec4, float *__restrict__ glo) {
+               float *__restrict__ grid, int vec4, float *__restrict__ glo,
+               const unsigned *__restrict__ cap_count, unsigned capT, unsigned ipt) {
     constexpr bool FIXED = ACC == kAccFixed;
     constexpr bool COMP = ACC == kAccComp;
     // Fewest fractional bits a fixed-point item may keep; an item whose bound
@@ -785,7 +1040,12 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
     // Nyquist wavenumber, so a PCS item takes fixed point only where its
     // quantization noise (64 taps of at most 2^-25 each per cell) stays
     // below that of float32 accumulation; tiles holding dense halos keep
-    // float atomics.
+    // float atomics.  TSC keeps fixed point at any scale: requiring 25 bits
+    // sent most 512^3 Zel'dovich tiles to float atomics (deposit 2.4 ->
+    // 5.8 ms) and left the corner bins where they were -- those bins hold a
+    // handful of modes and sit at the float32 noise of the FFT as much as of
+    // the grid (the last bin: 3e-5 to 3e-4 of P0 over deposit variants and
+    // runs, the reference's own summation orders 1e-5 to 5e-5).
     constexpr int MIN_BITS = MAS == PYL_MAS_PCS ? 24 : 0;
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
@@ -794,15 +1054,25 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
     __shared__ float s_max[32];
     const int RX = g.RX, RY = g.RY, RZ = g.RZ;
     const int cells = RX * RY * RZ;
-    const unsigned total = *nitems;
+    const unsigned total = cap_count ? (unsigned)g.ntiles * ipt : *nitems;
     for (unsigned it = blockIdx.x; it < total; it += gridDim.x) {
-        const uint2 item = items[it];
-        const int t = (int)item.x;
+        int t;
+        long long p0, p1;
+        if (cap_count) {
+            t = (int)(it / ipt);
+            const long long base = (long long)t * capT;
+            p0 = base + (long long)(it % ipt) * kItemCap;
+            p1 = min(base + (long long)min(cap_count[t], capT), p0 + (long long)kItemCap);
+            if (p0 >= p1) continue;          // the whole CTA skips an empty chunk
+        } else {
+            const uint2 item = items[it];
+            t = (int)item.x;
+            p0 = (long long)start[t] + (long long)item.y * kItemCap;
+            p1 = min((long long)start[t + 1], p0 + (long long)kItemCap);
+        }
         for (int i = threadIdx.x; i < (COMP ? 2 : 1) * cells; i += blockDim.x) s_reg[i] = 0.f;
         const int tx = t / (g.nty * g.ntz), ty = (t / g.ntz) % g.nty, tz = t % g.ntz;
         const int ox = tx * g.TX, oy = ty * g.TY, oz = tz * g.TZ;   // tile origin (cells)
-        const long long p0 = (long long)start[t] + (long long)item.y * kItemCap;
-        const long long p1 = min((long long)start[t + 1], p0 + (long long)kItemCap);
         __syncthreads();
         float scale = 1.f, inv_scale = 1.f;
         bool fixed = FIXED;   // this item in fixed point
@@ -844,9 +1114,9 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             // only, so R^3 times the largest home cell bounds every cell.
             // Where that bound leaves fewer than FAST_BITS fractional bits,
             // the box sums of the histogram give the tight bound.  TSC and
-            // PCS need 24 bits there: with R^3 = 64 the loose bound costs
-            // them about two bits, and the 512^3 TSC corner bins beyond the
-            // Nyquist wavenumber then moved from 1.4e-4 to 3.8e-4 of P0;
+            // PCS need 24 bits there: with R^3 = 27 or 64 the loose bound
+            // costs them about two bits, and the 512^3 TSC corner bins beyond
+            // the Nyquist wavenumber then moved from 1.4e-4 to 3.8e-4 of P0;
             // NGP / CIC keep the loose bound from 21 bits on (512^3 CIC:
             // worst bin 3.0e-6 -> 5.4e-6 of P0).
             constexpr int R = S::LO + S::HI + 1;
@@ -1170,6 +1440,124 @@ size_t partition_smem(bool weighted) {
            sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 4 * kMaxKeys;
 }
 
+// k_partition_cap: the same buffers, four per-key tables and the bucket
+// chunk prefix
+size_t partition_cap_smem(bool weighted) {
+    return sizeof(float) * (9 * (size_t)KP + (weighted ? 3 * (size_t)KP : 0)) +
+           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (5 * kMaxKeys + 1);
+}
+
+unsigned round_up4(double v) {
+    const unsigned u = (unsigned)ceil(v);
+    return (u + 3u) & ~3u;
+}
+
+// The count-free sort (see pyl_ctx::SortPlan): fixed slots of capT particles
+// per tile and capC per coarse bucket, sized from the occupancy the last
+// exact sort of the same kind showed, a spill list for what does not fit.
+template <int MAS, bool HAS_W>
+int launch_capacity_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
+                      float *grid, int dims, float inv, const TileGeom &g, int mode,
+                      unsigned capT, unsigned capC, int acc, int sms) {
+    int st = PYL_OK;
+    const int nt = g.ntiles;
+    const bool two_pass = mode != kSortFrontier;
+    unsigned *info = (unsigned *)ws_get(ctx, "dep_info", 4 * sizeof(unsigned), &st);
+    if (!info) return st;
+    unsigned *spill_n = info + 3;
+    unsigned *fcur = (unsigned *)ws_get(ctx, "dep_fcur", sizeof(unsigned) * (size_t)nt, &st);
+    if (!fcur) return st;
+    unsigned *ccur = (unsigned *)ws_get(ctx, "dep_ccur", sizeof(unsigned) * (size_t)g.ncoarse, &st);
+    if (!ccur) return st;
+    float *b1 = nullptr, *w1 = nullptr, *w2 = nullptr, *spw = nullptr;
+    const size_t nb1 = (size_t)g.ncoarse * capC, nb2 = (size_t)nt * capT;
+    if (two_pass) {
+        b1 = (float *)ws_get(ctx, "dep_b1", sizeof(float) * 3 * nb1, &st);
+        if (!b1) return st;
+    }
+    float *b2 = (float *)ws_get(ctx, "dep_b2", sizeof(float) * 3 * nb2, &st);
+    if (!b2) return st;
+    float *sp = (float *)ws_get(ctx, "dep_spill", sizeof(float) * 3 * (size_t)n, &st);
+    if (!sp) return st;
+    if (HAS_W) {
+        if (two_pass) {
+            w1 = (float *)ws_get(ctx, "dep_w1", sizeof(float) * nb1, &st);
+            if (!w1) return st;
+        }
+        w2 = (float *)ws_get(ctx, "dep_w2", sizeof(float) * nb2, &st);
+        if (!w2) return st;
+        spw = (float *)ws_get(ctx, "dep_spillw", sizeof(float) * (size_t)n, &st);
+        if (!spw) return st;
+    }
+    PYL_CUDA(ctx, cudaMemsetAsync(info, 0, 4 * sizeof(unsigned), ctx->stream));
+    PYL_CUDA(ctx, cudaMemsetAsync(fcur, 0, sizeof(unsigned) * (size_t)nt, ctx->stream));
+    {
+        StageScope s(ctx, ST_SORT);
+        if (two_pass) {
+            PYL_CUDA(ctx, cudaMemsetAsync(ccur, 0, sizeof(unsigned) * (size_t)g.ncoarse,
+                                          ctx->stream));
+            const size_t psm = partition_cap_smem(HAS_W);
+            if ((st = set_smem(ctx, k_partition_cap<MAS, HAS_W, false>, psm))) return st;
+            if ((st = set_smem(ctx, k_partition_cap<MAS, HAS_W, true>, psm))) return st;
+            static int per_sm = 0;
+            if (!per_sm) {
+                PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                  &per_sm, k_partition_cap<MAS, HAS_W, true>, kPartThreads, psm));
+                if (per_sm < 1) per_sm = 1;
+            }
+            const unsigned nblk = (unsigned)std::min<long long>((n + KP - 1) / KP,
+                                                                (long long)per_sm * sms);
+            const int bulk_in = ((uintptr_t)pos & 15) == 0 && (!W || ((uintptr_t)W & 15) == 0);
+            k_partition_cap<MAS, HAS_W, false><<<nblk, kPartThreads, psm, ctx->stream>>>(
+                pos, W, nullptr, 0u, n, b1, w1, capC, ccur, inv, g, bulk_in, sp, spw, spill_n,
+                ctx->d_status);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+            k_partition_cap<MAS, HAS_W, true><<<nblk, kPartThreads, psm, ctx->stream>>>(
+                b1, w1, ccur, capC, n, b2, w2, capT, fcur, inv, g, 1, sp, spw, spill_n,
+                ctx->d_status);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+        } else {
+            long long blocks = (n + 255) / 256;
+            if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+            k_scatter_frontier<MAS, HAS_W><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
+                pos, W, n, inv, g, fcur, b2, w2, nullptr, capT, sp, spw, spill_n);
+            ctx->launches++;
+            PYL_CUDA(ctx, cudaGetLastError());
+        }
+    }
+    const int vec4 = (dims % 4 == 0 && ((uintptr_t)grid & 15) == 0) ? 1 : 0;
+    const size_t rsm = sizeof(float) * (size_t)g.RX * g.RY * g.RZ;
+    const unsigned ipt = (capT + kItemCap - 1) / kItemCap;
+    auto run = [&](auto kernel) -> int {
+        int st2;
+        if ((st2 = set_smem(ctx, kernel, rsm))) return st2;
+        int per_sm = 0;
+        PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 512, rsm));
+        long long grid_n = (long long)(per_sm > 0 ? per_sm : 1) * sms * 4;
+        if (grid_n > (long long)nt * ipt) grid_n = (long long)nt * ipt;
+        if ((st2 = wait_grid(ctx))) return st2;
+        StageScope s(ctx, ST_DEPOSIT);
+        kernel<<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(b2, w2, nullptr, nullptr, nullptr, inv,
+                                                           g, grid, vec4, nullptr, fcur, capT, ipt);
+        ctx->launches++;
+        PYL_CUDA(ctx, cudaGetLastError());
+        return PYL_OK;
+    };
+    if ((st = acc == kAccFixed ? run(k_tile_deposit<MAS, HAS_W, kAccFixed>)
+                               : run(k_tile_deposit<MAS, HAS_W, kAccFloat>)))
+        return st;
+    // the particles beyond their slots (none unless the occupancy grew)
+    k_deposit_atomic<MAS, HAS_W, float, false><<<152 * 8, kThreads, 0, ctx->stream>>>(
+        sp, n, 3, spw, grid, dims, inv, nullptr, spill_n);
+    ctx->launches++;
+    PYL_CUDA(ctx, cudaGetLastError());
+    ctx->sort_used.cap = true;
+    ctx->d_sort_info = info;
+    return PYL_OK;
+}
+
 template <int MAS, bool HAS_W>
 int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W, float *grid,
                     int dims, float inv, const TileGeom &g, int forced_mode, int acc,
@@ -1194,6 +1582,8 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
     if (!items) return st;
     unsigned *nitems = (unsigned *)ws_get(ctx, "dep_nitems", sizeof(unsigned), &st);
     if (!nitems) return st;
+    unsigned *info = (unsigned *)ws_get(ctx, "dep_info", 4 * sizeof(unsigned), &st);
+    if (!info) return st;
     float *b1 = nullptr, *w1 = nullptr, *w2 = nullptr;
     if (two_pass) {
         b1 = (float *)ws_get(ctx, "dep_b1", sizeof(float) * 3 * (size_t)n, &st);
@@ -1215,6 +1605,7 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         StageScope s(ctx, ST_BINS);
         PYL_CUDA(ctx, cudaMemsetAsync(start, 0, sizeof(unsigned) * (size_t)(nt + 1), ctx->stream));
         PYL_CUDA(ctx, cudaMemsetAsync(flags2, 0, 2 * sizeof(unsigned), ctx->stream));
+        PYL_CUDA(ctx, cudaMemsetAsync(info, 0, 4 * sizeof(unsigned), ctx->stream));
         const size_t hsm = sizeof(unsigned) * (size_t)nt;
         if (((uintptr_t)pos & 15) == 0) {
             if ((st = set_smem(ctx, k_tile_count4<MAS>, hsm))) return st;
@@ -1230,7 +1621,7 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         if ((st = scan_exclusive(ctx, start, nt + 1))) return st;
         k_sort_setup<<<(nt + 255) / 256, 256, 0, ctx->stream>>>(start, nt, g.F, g.ncoarse, fcur,
                                                                 ccur, nchunk, n, distinct,
-                                                                forced_mode, mode);
+                                                                forced_mode, mode, info);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         PYL_CUDA(ctx, cudaMemsetAsync(nchunk + nt, 0, sizeof(unsigned), ctx->stream));
@@ -1270,7 +1661,7 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
             long long blocks = (n + 255) / 256;
             if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
             k_scatter_frontier<MAS, HAS_W><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
-                pos, W, n, inv, g, fcur, b2, w2, mode);
+                pos, W, n, inv, g, fcur, b2, w2, mode, 0u, nullptr, nullptr, nullptr);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
         }
@@ -1285,13 +1676,16 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         PYL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 512, rsm));
         long long grid_n = (long long)(per_sm > 0 ? per_sm : 1) * sms * 4;
         if (grid_n > (long long)max_items) grid_n = (long long)max_items;
+        if ((st2 = wait_grid(ctx))) return st2;
         StageScope s(ctx, ST_DEPOSIT);
         kernel<<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(b2, w2, start, items, nitems, inv, g,
-                                                           grid, vec4, glo);
+                                                           grid, vec4, glo, nullptr, 0u, 1u);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         return PYL_OK;
     };
+    ctx->sort_used.cap = false;
+    ctx->d_sort_info = info;
     if (acc == kAccComp) return run(k_tile_deposit<MAS, HAS_W, kAccComp>);
     if (acc == kAccFixed) return run(k_tile_deposit<MAS, HAS_W, kAccFixed>);
     return run(k_tile_deposit<MAS, HAS_W, kAccFloat>);
@@ -1307,6 +1701,29 @@ int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, f
     // scale keeps at least 24 fractional bits) unless float atomics are
     // asked for.
     const int acc = glo ? kAccComp : !(flags & PYL_DEPOSIT_FLOAT) ? kAccFixed : kAccFloat;
+    ctx->sort_used = pyl_ctx::SortUsed();
+    ctx->sort_used.valid = true;
+    ctx->sort_used.n = n;
+    ctx->sort_used.ntiles = g.ntiles;
+    ctx->sort_used.F = g.F;
+    ctx->sort_used.plan = ctx->sort_hint;
+    // the count-free sort where the last request of this kind allows it
+    const pyl_ctx::SortPlan *plan = ctx->sort_hint;
+    if (plan && plan->cap && acc != kAccComp) {
+        const double mean_t = (double)n / g.ntiles;
+        const unsigned capT = round_up4(plan->phiT * mean_t + 32.0);
+        const unsigned capC = round_up4(plan->phiC * mean_t * g.F + KP);
+        const int mode = forced >= 0 ? forced : plan->mode;
+        if ((double)capT * g.ntiles < 4.0e9 && (double)capC * g.ncoarse < 4.0e9 &&
+            (mode == kSortFrontier || mode == kSortTwoPass)) {
+            int sms = 152;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+            return W ? launch_capacity_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, mode, capT,
+                                                    capC, acc, sms)
+                     : launch_capacity_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, mode,
+                                                     capT, capC, acc, sms);
+        }
+    }
     return W ? launch_sorted_t<MAS, true>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo)
              : launch_sorted_t<MAS, false>(ctx, pos, n, W, grid, dims, inv, g, forced, acc, glo);
 }
@@ -1331,6 +1748,7 @@ static int deposit_t(pyl_ctx *ctx, const float *pos, int64_t n, int coord, const
                      G *grid, int dims, float BoxSize, int mas, int flags) {
     if (mas < PYL_MAS_NGP || mas > PYL_MAS_PCS)
         return fail(ctx, PYL_ERR_ARG, "option not valid!!! (MAS must be NGP, CIC, TSC or PCS)");
+    ctx->sort_used = pyl_ctx::SortUsed();   // set by the sorted path below
     if (n == 0) return PYL_OK;
     // inv_cell_size = dims/BoxSize as a float division (MAS_library.pyx:135)
     const float inv = (float)dims / BoxSize;

@@ -62,14 +62,16 @@ k_pk_x_p2(const float2 *__restrict__ data, int h, int rs, const float2 *__restri
         {
             const int cc = threadIdx.x / P, rr = threadIdx.x % P;
             const int kzc = (it % nzb) * C + cc;
+            RunAcc R;
             if (kzc < h) {
                 const float2 *ln = sm + N + cc * LINE;
                 const int ky = kyy > MID ? kyy - N : kyy;
                 const float wyz = win[pad8(kyy)] * win[pad8(kzc)];
                 constexpr int E = RegPlan<N>::E;
-                bin_run<WHAT, E>(H, acc, ln, [](int i) { return pad8(i); }, E * rr, ky, kzc, N,
-                                 axis, win, wyz, MID);
+                bin_run<WHAT, E>(R, H, acc, ln, [](int i) { return pad8(i); }, E * rr, ky, kzc,
+                                 N, axis, win, wyz, MID);
             }
+            warp_flush_runs(H, R);   // every lane of the warp, valid column or not
         }
         __syncthreads();   // the shared lines are reused by the next item
     }

@@ -80,77 +80,112 @@ __device__ __forceinline__ void mode_extras(Hist &H, const PkAcc &acc, int n2, i
     }
 }
 
-// Register run of consecutive modes that fall into the same |k| bin: the
-// three multipole sums are kept in registers and added to the shared
-// histogram once per run.
-struct BinRun {
-    int bin = -1;
-    float p0 = 0.f, p2 = 0.f, p4 = 0.f;
-    template <class Hist>
-    __device__ __forceinline__ void flush(Hist &H) {
-        if (bin >= 0) {
-            atomicAdd(&H.h3[3 * bin + 0], p0);
-            atomicAdd(&H.h3[3 * bin + 1], p2);
-            atomicAdd(&H.h3[3 * bin + 2], p4);
-        }
-        bin = -1;
-        p0 = p2 = p4 = 0.f;
-    }
+// Runs of consecutive modes of one lane that fall into the same |k| bin:
+// the multipole sums of the current run are kept in registers.  The lane's
+// first run (head) and its last run (tail) may continue in the neighbouring
+// lanes' modes, so they are kept for the warp merge (warp_flush_runs); the
+// runs in between are complete and go to the shared histogram as they close.
+struct RunAcc {
+    int hb = -1, cb = -1;                 // head bin, current (tail) bin; -1: none
+    float h0 = 0.f, h1 = 0.f, h2 = 0.f;
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
     template <class Hist>
     __device__ __forceinline__ void add(Hist &H, int b, float d2, float mu2) {
-        if (b != bin) {
-            flush(H);
-            bin = b;
+        if (b != cb) {
+            if (cb >= 0) {
+                if (hb < 0) {
+                    hb = cb;
+                    h0 = c0; h1 = c1; h2 = c2;
+                } else {
+                    atomicAdd(&H.h3[3 * cb + 0], c0);
+                    atomicAdd(&H.h3[3 * cb + 1], c1);
+                    atomicAdd(&H.h3[3 * cb + 2], c2);
+                }
+            }
+            cb = b;
+            c0 = c1 = c2 = 0.f;
         }
-        p0 += d2;
-        p2 += d2 * (3.f * mu2 - 1.f) * 0.5f;
-        p4 += d2 * ((35.f * mu2 - 30.f) * mu2 + 3.f) * 0.125f;
+        c0 += d2;
+        c1 += d2 * (3.f * mu2 - 1.f) * 0.5f;
+        c2 += d2 * ((35.f * mu2 - 30.f) * mu2 + 3.f) * 0.125f;
     }
 };
 
-// Same per-mode work as bin_mode, accumulating the multipoles into a run.
-template <int WHAT, class Hist>
-__device__ __forceinline__ void bin_mode_run(BinRun &R, Hist &H, const PkAcc &acc, float2 v,
-                                             int kxx, int ky, int kz, int n, int axis, float wx,
-                                             float wyz, int mid) {
-    const bool even = (n & 1) == 0;
-    const int kx = kxx > mid ? kxx - n : kxx;
-    if (kz == 0 || (kz == mid && even)) {
-        if (kx < 0) return;
-        if (kx == 0 || (kx == mid && even)) {
-            if (ky < 0) return;
+// Adds the head and tail runs of the 32 lanes of a warp to the shared
+// histogram, merging runs of neighbouring lanes that share a bin first, so
+// that lanes hitting one bin (along a pencil |k| often changes by less than
+// one over many modes) make one set of shared atomics instead of one each.
+// A segmented inclusive scan over the lanes sums the tails of each maximal
+// stretch of lanes whose tails share a bin (a lane with a head run starts a
+// new stretch); the last lane of a stretch also takes the next lane's head
+// when its bin matches, and adds the total.  Every run is added exactly once
+// whatever the bins are.  Every thread of the warp must call it (a CTA of
+// fewer than 32 threads, as for 16-point lines, is one partial warp).
+template <class Hist>
+__device__ __forceinline__ void warp_flush_runs(Hist &H, const RunAcc &R) {
+    const int lane = threadIdx.x & 31;
+    const int nl = min(32, (int)blockDim.x - (int)(threadIdx.x & ~31u));   // lanes present
+    const unsigned FULL = nl == 32 ? 0xffffffffu : ((1u << nl) - 1u);
+    const int last = nl - 1;
+    const int prev_tb = __shfl_up_sync(FULL, R.cb, 1);
+    const int start = (lane == 0 || R.hb >= 0 || R.cb < 0 || R.cb != prev_tb) ? 1 : 0;
+    float v0 = R.c0, v1 = R.c1, v2 = R.c2;
+    int f = start;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float u0 = __shfl_up_sync(FULL, v0, d);
+        const float u1 = __shfl_up_sync(FULL, v1, d);
+        const float u2 = __shfl_up_sync(FULL, v2, d);
+        const int uf = __shfl_up_sync(FULL, f, d);
+        if (lane >= d) {
+            if (!f) {
+                v0 += u0;
+                v1 += u1;
+                v2 += u2;
+            }
+            f |= uf;
         }
     }
-    if (kx == 0 && ky == 0 && kz == 0) *acc.dc = v;
-    const int n2 = kx * kx + ky * ky + kz * kz;
-    const int bin = isqrt_dev(n2);
-    const int kpar = axis == 0 ? kx : (axis == 1 ? ky : kz);
-    const float f = wx * wyz;
-    const float re = v.x * f, im = v.y * f;
-    const float d2 = re * re + im * im;
-    const float mu2 = n2 > 0 ? (float)(kpar * kpar) / (float)n2 : 0.f;
-    R.add(H, bin, d2, mu2);
-    if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
+    const int next_start = __shfl_down_sync(FULL, start, 1);
+    const int nb = __shfl_down_sync(FULL, R.hb, 1);
+    const float n0 = __shfl_down_sync(FULL, R.h0, 1);
+    const float n1 = __shfl_down_sync(FULL, R.h1, 1);
+    const float n2 = __shfl_down_sync(FULL, R.h2, 1);
+    if (R.cb >= 0 && (lane == last || next_start)) {
+        if (lane < last && nb == R.cb) {     // the next lane's head continues this stretch
+            v0 += n0;
+            v1 += n1;
+            v2 += n2;
+        }
+        atomicAdd(&H.h3[3 * R.cb + 0], v0);
+        atomicAdd(&H.h3[3 * R.cb + 1], v1);
+        atomicAdd(&H.h3[3 * R.cb + 2], v2);
+    }
+    if (R.hb >= 0 && !(lane > 0 && R.hb == prev_tb)) {
+        atomicAdd(&H.h3[3 * R.hb + 0], R.h0);
+        atomicAdd(&H.h3[3 * R.hb + 1], R.h1);
+        atomicAdd(&H.h3[3 * R.hb + 2], R.h2);
+    }
 }
 
 // L consecutive modes kxx0 .. kxx0+L-1 of one pencil (ky, kz fixed), read
 // from shared memory at ln[pad(kxx)], the window at win[pad(kxx)] (the pad
-// spreads the L-strided accesses of a warp over the banks): the same work as
-// bin_mode_run, with the bin index updated incrementally instead of one
+// spreads the L-strided accesses of a warp over the banks): the per-mode
+// work of bin_mode, into the lane's runs R (the caller ends with
+// warp_flush_runs), with the bin index updated incrementally instead of one
 // square root per mode.  Between neighbours |kx| changes by one, so
 // sqrt(kx^2 + ky^2 + kz^2) changes by at most one and the bin by -1, 0 or +1.
 // Pencils off the kz = 0 and kz = mid planes (all but two planes) need none
 // of the half-space checks and hold no DC mode: they take a branch-free body.
 template <int WHAT, int L, class Hist, class Pad>
-__device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 *ln, Pad pad,
-                                         int kxx0, int ky, int kz, int n, int axis,
-                                         const float *win, float wyz, int mid) {
+__device__ __forceinline__ void bin_run(RunAcc &R, Hist &H, const PkAcc &acc, const float2 *ln,
+                                        Pad pad, int kxx0, int ky, int kz, int n, int axis,
+                                        const float *win, float wyz, int mid) {
     const bool even = (n & 1) == 0;
     const bool plane = (kz == 0 || (kz == mid && even));
     const int r2 = ky * ky + kz * kz;
     const int kx0 = kxx0 > mid ? kxx0 - n : kxx0;
     int bin = isqrt_dev(kx0 * kx0 + r2);
-    BinRun R;
     if (!plane) {
         const int kpar_c = axis == 1 ? ky : kz;   // kpar when it is not kx
 #pragma unroll
@@ -168,7 +203,6 @@ __device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 
             R.add(H, bin, d2, mu2);
             if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
         }
-        R.flush(H);
         return;
     }
 #pragma unroll
@@ -189,7 +223,6 @@ __device__ __forceinline__ void bin_run(Hist &H, const PkAcc &acc, const float2 
         R.add(H, bin, d2, mu2);
         if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
     }
-    R.flush(H);
 }
 
 // Float32-only shared histograms of one CTA, added to the global float64
