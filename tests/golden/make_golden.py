@@ -58,8 +58,8 @@ def edge_positions(dims, coord):
 
 
 def main():
-    build_ref.build("/root/reference") if not os.path.isdir(
-        os.path.join(ROOT, "oracle", "_ref")) else None
+    if not build_ref.built():
+        build_ref.build(build_ref.default_reference())   # $PYLIANS3_REFERENCE or the default
     MASL, PKL = build_ref.load()
     rng = np.random.default_rng(20261203)
 

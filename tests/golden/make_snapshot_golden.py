@@ -21,7 +21,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "snapshots")
-REF = "/root/reference/library"
+# the reference tree: $PYLIANS3_REFERENCE (default /root/reference)
+REF = os.path.join(os.environ.get("PYLIANS3_REFERENCE", "/root/reference"), "library")
 
 
 def write_snapshot(path, end, fmt, npart, nall, massarr, time, redshift, filenum, box,
