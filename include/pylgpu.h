@@ -243,15 +243,20 @@ typedef struct {
     int mas_deposit, axis, mas_window, what;
 } pyl_pk_request;
 
-/* Spectra of `count` requests issued back to back on the context stream and
- * waited for once (no reference counterpart: the batched form of
- * pyl_pk_particles).  The sequence is captured into a CUDA graph the first
- * time a given list of requests (same pointers, sizes and options) is seen
- * -- that first call issues the requests directly, which also sizes the
- * workspaces -- and later calls with the same list launch the graph: one
- * launch for the whole batch.  outs[i] receives request i (arrays as for
- * pyl_pk).  All requests use device pointers (PYL_DEVICE_PTRS) or all host
- * pointers; PYL_NO_GRAPH skips the graph.                                  */
+/* Spectra of `count` requests issued at once and waited for once (no
+ * reference counterpart: the batched form of pyl_pk_particles).  The
+ * requests are spread over lanes -- child contexts with their own streams
+ * and workspaces that run side by side (PYL_BATCH_LANES(k) in flags, 1..15;
+ * 0 = 4 lanes) -- longest first onto the least loaded lane.  The sequence is
+ * captured into a CUDA graph (the lanes as parallel branches) the first
+ * time a given list of requests (same pointers, sizes and options) is seen:
+ * that first call issues the requests directly with the exact counting sort,
+ * which also sizes the workspaces, and learns from each request the slots of
+ * the count-free sort the graph then uses; later calls with the same list
+ * launch the graph: one launch for the whole batch.  outs[i] receives
+ * request i (arrays as for pyl_pk).  All requests use device pointers
+ * (PYL_DEVICE_PTRS) or all host pointers; PYL_NO_GRAPH skips the graph.     */
+#define PYL_BATCH_LANES(k) (((k) & 0xF) << 16)
 int pyl_pk_batch(pyl_ctx *ctx, const pyl_pk_request *reqs, int count,
                  pyl_pk_out *outs, int flags);
 

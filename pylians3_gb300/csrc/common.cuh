@@ -139,6 +139,17 @@ struct pyl_ctx {
     // reallocation synchronises the stream); the last captured batch, its
     // key (the request list and flags) and the pinned buffer it writes.
     bool capturing = false;
+    // pyl_pk_batch's lanes: child contexts (own stream, own workspaces) whose
+    // requests run side by side, forked from and joined back to this
+    // context's stream by events; the sort plans learned per request of the
+    // batch (keyed by batch_plans_key) and the sorts its graph was captured
+    // with (batch_used).
+    std::vector<pyl_ctx *> lanes;
+    std::vector<cudaEvent_t> lane_join;
+    cudaEvent_t lane_fork = nullptr;
+    std::vector<SortPlan> batch_plans;
+    std::vector<char> batch_plans_key;
+    std::vector<SortUsed> batch_used;
     cudaGraphExec_t batch_exec = nullptr;
     std::vector<char> batch_key;
     void *batch_pinned = nullptr;
@@ -280,6 +291,12 @@ int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, 
                     void *dst);
 int finalize_particles(pyl_ctx *ctx, const ModeTables &T, const AccLayout &L, const void *src,
                        int dims, double BoxSize, int what, pyl_pk_out *out);
+// Bytes a request's result takes in pinned memory: the raw sums, the k = 0
+// mode, the mass and the 4 info words of its sort (copied when the request
+// was issued with a sort plan).
+size_t result_bytes(const AccLayout &L);
+// Updates the sort plan of a finished request from its sort's info words.
+void learn_sort(const pyl_ctx::SortUsed &u, const unsigned *info);
 void twiddles_host(int n, std::vector<float2> &tw);
 void window_host(int dims, int mas, std::vector<float> &w);
 // Mode tables: sizes of the count arrays, and the tables from the counts.

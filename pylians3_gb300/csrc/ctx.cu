@@ -331,6 +331,7 @@ int pyl_ctx_create(pyl_ctx **out, int device, void *stream) {
 }
 
 static void release_all(pyl_ctx *ctx) {
+    for (pyl_ctx *c : ctx->lanes) release_all(c);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     cudaStreamSynchronize(ctx->stream);
     for (auto &kv : ctx->ws) if (kv.second.p) cudaFree(kv.second.p);
@@ -351,6 +352,9 @@ int pyl_ctx_destroy(pyl_ctx *ctx) {
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
     if (ctx->batch_pinned) cudaFreeHost(ctx->batch_pinned);
+    for (pyl_ctx *c : ctx->lanes) pyl_ctx_destroy(c);
+    for (cudaEvent_t e : ctx->lane_join) cudaEventDestroy(e);
+    if (ctx->lane_fork) cudaEventDestroy(ctx->lane_fork);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
@@ -392,6 +396,8 @@ int pyl_ctx_workspace_bytes(const pyl_ctx *ctx, size_t *bytes) {
     if (!ctx || !bytes) return PYL_ERR_ARG;
     size_t s = 0;
     for (auto &kv : ctx->ws) s += kv.second.bytes;
+    for (const pyl_ctx *c : ctx->lanes)
+        for (auto &kv : c->ws) s += kv.second.bytes;
     *bytes = s;
     return PYL_OK;
 }
@@ -789,6 +795,10 @@ int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, 
 // an exact sort, slots sized from the largest tile and bucket counts (with a
 // margin) unless the input is clustered; after a count-free sort whose slots
 // overflowed, the exact sort again.
+size_t result_bytes(const AccLayout &L) {
+    return L.sums() + sizeof(float2) + sizeof(double) + 4 * sizeof(unsigned);
+}
+
 void learn_sort(const pyl_ctx::SortUsed &u, const unsigned *info) {
     if (!u.valid || !u.plan) return;
     pyl_ctx::SortPlan &p = *u.plan;

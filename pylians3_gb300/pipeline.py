@@ -145,9 +145,10 @@ def power_spectra(pos_sets, dims, BoxSize, MAS="CIC", axis=2, W_sets=None, windo
     return results
 
 
-def spectra_batch(requests, ctx=None, graph=True):
-    """Spectra of a list of requests issued back to back and waited for once
-    (pyl_pk_batch): the first call with a given list captures the launch
+def spectra_batch(requests, ctx=None, graph=True, lanes=0):
+    """Spectra of a list of requests issued at once and waited for once
+    (pyl_pk_batch), spread over ``lanes`` streams that run side by side
+    (0: the library's default, 4): the first call with a given list captures the launch
     sequence into a CUDA graph, later calls with the same list (same arrays,
     sizes and options) launch it as one graph.  requests: dicts with the
     arguments of ``power_spectrum`` (pos, dims, BoxSize, MAS, axis, W,
@@ -184,7 +185,8 @@ def spectra_batch(requests, ctx=None, graph=True):
                                     int(r.get("axis", 2)), win, int(r.get("what", 0)))
     if ctx is None:
         ctx = _native.context(requests[0]["pos"].device.index or 0 if dev else 0)
-    flags = (_native.PYL_DEVICE_PTRS if dev else 0) | (0 if graph else _native.PYL_NO_GRAPH)
+    flags = ((_native.PYL_DEVICE_PTRS if dev else 0) | (0 if graph else _native.PYL_NO_GRAPH)
+             | ((int(lanes) & 0xF) << 16))
     _raise_or_exit(ctx, ctx.lib.pyl_pk_batch(ctx.ptr, reqs, len(requests), outa, flags))
     res = []
     for o in outs:

@@ -158,3 +158,78 @@ def test_spectra_batch_graph_equals_single_calls(env):
             err = np.abs(x.Pk - one.Pk).max(axis=1) / np.abs(one.Pk[:, 0])
             assert err[:r["dims"] // 2 + 1].max() <= TOL_PK
     ctx.close()
+
+
+def _batch_requests(torch, seed, count=10):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        dims = int(rng.choice([96, 128, 192]))
+        n = int(dims ** 3 * rng.integers(1, 4))
+        W = None
+        if i % 3 == 1:
+            g = torch.Generator(device="cuda").manual_seed(seed + 50 + i)
+            W = torch.exp(0.5 * torch.randn(n, generator=g, device="cuda"))
+        reqs.append(dict(pos=make_pos(torch, n, seed + i), dims=dims, BoxSize=BOX, W=W,
+                         MAS=str(rng.choice(["CIC", "TSC"])), axis=int(rng.integers(0, 3))))
+    return reqs
+
+
+@pytest.mark.parametrize("lanes", [1, 3, 4])
+def test_batch_lanes_and_learned_sorts(env, lanes):
+    """The batch over 1, 3 or 4 lanes: the direct first call (exact sorts),
+    the graph relaunches (count-free sorts learned from the first call) and
+    one-at-a-time calls give the same spectra."""
+    torch, native, P = env
+    from pylians3_gb300.pipeline import spectra_batch
+    reqs = _batch_requests(torch, 40 + lanes)
+    ctx = native.Context(0)
+    first = spectra_batch(reqs, ctx=ctx, lanes=lanes)
+    again = spectra_batch(reqs, ctx=ctx, lanes=lanes)
+    third = spectra_batch(reqs, ctx=ctx, lanes=lanes)
+    for r, a, b, c in zip(reqs, first, again, third):
+        one = P.power_spectrum(**r)
+        for x in (a, b, c):
+            assert np.array_equal(x.Nmodes3D, one.Nmodes3D)
+            err = np.abs(x.Pk - one.Pk).max(axis=1) / np.abs(one.Pk[:, 0])
+            assert err[:r["dims"] // 2 + 1].max() <= TOL_PK
+    ctx.close()
+
+
+def test_batch_graph_with_new_contents_stays_exact(env, oracle):
+    """A graph replay whose inputs changed in place (same pointers, clustered
+    contents) overflows the count-free slots learned from the old contents:
+    the spill deposit keeps the spectra exact, and the next calls learn and
+    capture again."""
+    torch, native, P = env
+    from pylians3_gb300.pipeline import spectra_batch
+    reqs = _batch_requests(torch, 77, count=4)
+    for r in reqs:
+        r["W"] = None
+        r["MAS"] = "CIC"
+    ctx = native.Context(0)
+    spectra_batch(reqs, ctx=ctx)                    # learn + capture on uniform contents
+    spectra_batch(reqs, ctx=ctx)
+    rng = np.random.default_rng(5)
+    for r in reqs:                                  # a third of each set into 20 clumps
+        n = int(r["pos"].shape[0])
+        k = n // 3
+        c = rng.random((20, 3)) * BOX
+        clump = np.mod(c[rng.integers(0, 20, k)] + rng.standard_normal((k, 3)) * 5.0, BOX)
+        r["pos"][:k] = torch.from_numpy(clump.astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    replay = spectra_batch(reqs, ctx=ctx)           # overflowing slots: spill deposit
+    relearn = spectra_batch(reqs, ctx=ctx)          # direct again, then recaptured
+    regraph = spectra_batch(reqs, ctx=ctx)
+    for r, a, b, c in zip(reqs, replay, relearn, regraph):
+        d = np.zeros((r["dims"],) * 3, np.float32)
+        pos = r["pos"].cpu().numpy()
+        oracle.MA(pos, d, BOX, "CIC")
+        d /= np.mean(d, dtype=np.float64)
+        d -= 1.0
+        ref = oracle.Pk(d, BOX, axis=r["axis"], MAS="CIC", threads=8)
+        for x in (a, b, c):
+            assert np.array_equal(x.Nmodes3D, ref.Nmodes3D)
+            err = np.abs(x.Pk - ref.Pk).max(axis=1) / np.abs(ref.Pk[:, 0])
+            assert err[:r["dims"] // 2].max() <= TOL_PK
+    ctx.close()
