@@ -66,6 +66,10 @@ enum { PYL_MAS_NONE = 0, PYL_MAS_NGP = 1, PYL_MAS_CIC = 2, PYL_MAS_TSC = 3,
 /* pyl_pk_batch: issue the requests directly instead of through the cached
  * CUDA graph (the same work, launch by launch).                           */
 #define PYL_NO_GRAPH       0x80
+/* pyl_pk_particles: sort with the exact counting sort even where the
+ * previous request of the same kind would allow the count-free one (see
+ * pyl_ctx_last_sort).                                                     */
+#define PYL_SORT_EXACT     0x100
 
 /* Which Pk outputs to compute (bit mask); the 3D multipoles always are.   */
 #define PYL_PK_3D     0x00

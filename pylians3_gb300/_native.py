@@ -34,6 +34,7 @@ PYL_SORT_TWO_PASS = 0x10
 PYL_SORT_FRONTIER = 0x20
 PYL_DEPOSIT_FLOAT = 0x40
 PYL_NO_GRAPH = 0x80
+PYL_SORT_EXACT = 0x100
 PYL_PK_1D, PYL_PK_2D, PYL_PK_PHASE, PYL_PK_ALL = 0x01, 0x02, 0x04, 0x07
 
 # every symbol include/pylgpu.h declares (checked by the tests)

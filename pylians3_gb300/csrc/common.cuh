@@ -87,14 +87,15 @@ struct pyl_ctx {
     int64_t stage_n[ST_NSTAGES] = {};
 
     // Count-free ("capacity") tile sort of the fused particles path: per
-    // (dims, scheme, weighted), what the last request showed.  After an
-    // exact sort, the largest tile and coarse-bucket counts relative to
-    // their means (phiT, phiC) size fixed slots for the next request, which
-    // then needs no counting pass; a request whose slots overflowed (its
-    // particles went to the spill list) sends the next one back to the
-    // exact sort.  mode: the sort the exact pass chose (frontier/two-pass).
+    // (device, dims, scheme, weighted), what the last request showed, shared
+    // by all contexts of the process (shared_sort_plan).  After an exact
+    // sort, the largest tile and coarse-bucket counts relative to their means
+    // (phiT, phiC) size fixed slots for the next request, which then needs
+    // no counting pass; a request whose slots overflowed (its particles went
+    // to the spill list) sends the next one back to the exact sort.  mode:
+    // the sort the exact pass chose (frontier/two-pass).  Plans are read and
+    // written under one lock (read_sort_plan, learn_sort).
     struct SortPlan { bool cap = false; float phiT = 0.f, phiC = 0.f; int mode = -1; };
-    std::map<std::tuple<int, int, int>, SortPlan> sort_plans;
     SortPlan *sort_hint = nullptr;     // set by the particles path around deposit()
     struct SortUsed {
         bool valid = false, cap = false;
@@ -297,6 +298,10 @@ int finalize_particles(pyl_ctx *ctx, const ModeTables &T, const AccLayout &L, co
 size_t result_bytes(const AccLayout &L);
 // Updates the sort plan of a finished request from its sort's info words.
 void learn_sort(const pyl_ctx::SortUsed &u, const unsigned *info);
+// The process-wide plan of (device, dims, scheme, weighted) (a stable
+// pointer), and a copy of a plan taken under the plans' lock.
+pyl_ctx::SortPlan *shared_sort_plan(int device, int dims, int mas, int weighted);
+pyl_ctx::SortPlan read_sort_plan(const pyl_ctx::SortPlan *p);
 void twiddles_host(int n, std::vector<float2> &tw);
 void window_host(int dims, int mas, std::vector<float> &w);
 // Mode tables: sizes of the count arrays, and the tables from the counts.

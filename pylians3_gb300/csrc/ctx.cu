@@ -799,8 +799,22 @@ size_t result_bytes(const AccLayout &L) {
     return L.sums() + sizeof(float2) + sizeof(double) + 4 * sizeof(unsigned);
 }
 
+static std::mutex g_plans_mu;
+static std::map<std::tuple<int, int, int, int>, pyl_ctx::SortPlan> g_plans;
+
+pyl_ctx::SortPlan *shared_sort_plan(int device, int dims, int mas, int weighted) {
+    std::lock_guard<std::mutex> lock(g_plans_mu);
+    return &g_plans[std::make_tuple(device, dims, mas, weighted)];
+}
+
+pyl_ctx::SortPlan read_sort_plan(const pyl_ctx::SortPlan *p) {
+    std::lock_guard<std::mutex> lock(g_plans_mu);
+    return *p;
+}
+
 void learn_sort(const pyl_ctx::SortUsed &u, const unsigned *info) {
     if (!u.valid || !u.plan) return;
+    std::lock_guard<std::mutex> lock(g_plans_mu);
     pyl_ctx::SortPlan &p = *u.plan;
     if (u.cap) {
         if (info[3] != 0) p.cap = false;
@@ -917,7 +931,7 @@ int pyl_pk_particles_enqueue(pyl_ctx *ctx, const float *pos, int64_t n, const fl
         ctx->pinned_bytes = nb;
     }
     if (!ctx->done) PYL_CUDA(ctx, cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming));
-    ctx->sort_hint = &ctx->sort_plans[std::make_tuple(dims, mas_deposit, W ? 1 : 0)];
+    ctx->sort_hint = shared_sort_plan(ctx->device, dims, mas_deposit, W ? 1 : 0);
     st = issue_particles(ctx, r, *T, flags, ctx->pinned);
     ctx->sort_hint = nullptr;
     if (st) return st;

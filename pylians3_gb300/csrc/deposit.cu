@@ -1708,12 +1708,13 @@ int launch_sorted(pyl_ctx *ctx, const float *pos, long long n, const float *W, f
     ctx->sort_used.F = g.F;
     ctx->sort_used.plan = ctx->sort_hint;
     // the count-free sort where the last request of this kind allows it
-    const pyl_ctx::SortPlan *plan = ctx->sort_hint;
-    if (plan && plan->cap && acc != kAccComp) {
+    const pyl_ctx::SortPlan plan = ctx->sort_hint ? read_sort_plan(ctx->sort_hint)
+                                                  : pyl_ctx::SortPlan();
+    if (plan.cap && acc != kAccComp && !(flags & PYL_SORT_EXACT)) {
         const double mean_t = (double)n / g.ntiles;
-        const unsigned capT = round_up4(plan->phiT * mean_t + 32.0);
-        const unsigned capC = round_up4(plan->phiC * mean_t * g.F + KP);
-        const int mode = forced >= 0 ? forced : plan->mode;
+        const unsigned capT = round_up4(plan.phiT * mean_t + 32.0);
+        const unsigned capC = round_up4(plan.phiC * mean_t * g.F + KP);
+        const int mode = forced >= 0 ? forced : plan.mode;
         if ((double)capT * g.ntiles < 4.0e9 && (double)capC * g.ncoarse < 4.0e9 &&
             (mode == kSortFrontier || mode == kSortTwoPass)) {
             int sms = 152;

@@ -34,7 +34,7 @@ DEPOSIT_FLAGS = {
 
 
 def power_spectrum(pos, dims, BoxSize, MAS="CIC", axis=2, W=None, window=None,
-                   what=0, ctx=None, deposit="auto"):
+                   what=0, ctx=None, deposit="auto", sort="auto"):
     """Spectrum of the particles' overdensity field on a dims^3 grid.
 
     pos: (n, 3) float32 numpy array (pinned memory copies fastest, see
@@ -42,6 +42,9 @@ def power_spectrum(pos, dims, BoxSize, MAS="CIC", axis=2, W=None, window=None,
     ``window`` the window to deconvolve (default: the same as MAS).
     ``what``: extra outputs (Pk_library.PK_1D | PK_2D | PK_PHASE).
     ``deposit``: accumulation of the grid, one of DEPOSIT_FLAGS.
+    ``sort``: "auto" takes the count-free tile sort where the previous
+    request of the same dims, scheme and weighting allows it; "exact" always
+    counts first.
     """
     require_dtype(pos, "float32", "pos")
     if pos.ndim != 2 or int(pos.shape[1]) != 3:
@@ -55,6 +58,10 @@ def power_spectrum(pos, dims, BoxSize, MAS="CIC", axis=2, W=None, window=None,
     if deposit not in DEPOSIT_FLAGS:
         raise ValueError("deposit must be one of %s" % sorted(DEPOSIT_FLAGS))
     dflags = DEPOSIT_FLAGS[deposit]
+    if sort not in ("auto", "exact"):
+        raise ValueError('sort must be "auto" or "exact"')
+    if sort == "exact":
+        dflags |= _native.PYL_SORT_EXACT
     out = _Outputs(int(dims), what)
     if is_cuda_tensor(pos):
         ctx = ctx or _native.context(pos.device.index or 0)

@@ -39,12 +39,14 @@ from .Pk_library import MAS_function, _Outputs
 
 
 def request_bytes(n: int, dims: int, weighted: bool, host_positions: bool) -> int:
-    """Device bytes a request needs in a slot (both sort buffers, grid,
-    half-complex grid, staging of host positions, small tables)."""
+    """Device bytes a request needs in a slot: the sort buffers (the
+    count-free sort's coarse and tile slots with their margins and its spill
+    list: about 3.2 records per particle), grid, half-complex grid, staging
+    of host positions, small tables."""
     rs = (dims // 2 + 1 + 7) // 8 * 8
-    b = 12 * n * 2 + 4 * dims ** 3 + 8 * dims * dims * rs + (64 << 20)
+    b = int(12 * n * 3.2) + 4 * dims ** 3 + 8 * dims * dims * rs + (64 << 20)
     if weighted:
-        b += 8 * n
+        b += int(4 * n * 3.2)
     if host_positions:
         b += 12 * n + (4 * n if weighted else 0)
     return b

@@ -1,8 +1,9 @@
 """The count-free tile sort of the fused particles path.
 
 After an exact (counting) sort, the next request of the same dims, scheme
-and weighting takes fixed slots sized from the occupancy the exact sort saw,
-and needs no counting pass.  Checked through the public API and
+and weighting (in any context of the process) takes fixed slots sized from
+the occupancy the exact sort saw, and needs no counting pass.  Checked
+through the public API (sort="exact" forces the counting sort) and
 pyl_ctx_last_sort:
   * on uniform input the count-free sort runs without spilling and gives the
     exact sort's spectrum to 1e-5 of P0 per bin (the grid differs by float32
@@ -34,8 +35,8 @@ def P():
     return P
 
 
-def spectra(P, ctx, pos, dims, MAS, axis, W=None):
-    s = P.power_spectrum(pos, dims, BOX, MAS, axis=axis, W=W, ctx=ctx)
+def spectra(P, ctx, pos, dims, MAS, axis, W=None, sort="auto"):
+    s = P.power_spectrum(pos, dims, BOX, MAS, axis=axis, W=W, ctx=ctx, sort=sort)
     return s, ctx.last_sort()
 
 
@@ -50,7 +51,7 @@ def test_uniform_count_free_equals_exact(P, MAS, weighted):
     if weighted:
         g = torch.Generator(device="cuda").manual_seed(12)
         W = torch.exp(0.5 * torch.randn(pos.shape[0], generator=g, device="cuda"))
-    a, (cf0, _) = spectra(P, ctx, pos, dims, MAS, 0, W)
+    a, (cf0, _) = spectra(P, ctx, pos, dims, MAS, 0, W, sort="exact")   # learns the slots
     b, (cf1, sp1) = spectra(P, ctx, pos, dims, MAS, 0, W)
     c, (cf2, sp2) = spectra(P, ctx, pos, dims, MAS, 0, W)
     assert cf0 == 0 and cf1 == 1 and cf2 == 1 and sp1 == 0 and sp2 == 0
@@ -67,7 +68,7 @@ def test_lattice_count_free_frontier_equals_exact(P):
     ctx = _native.Context(0)
     dims = 128
     pos = synth.zeldovich(dims, BOX, sigma=3.0, seed=5)      # lattice order: frontier sort
-    a, (cf0, _) = spectra(P, ctx, pos, dims, "CIC", 2)
+    a, (cf0, _) = spectra(P, ctx, pos, dims, "CIC", 2, sort="exact")
     b, (cf1, sp1) = spectra(P, ctx, pos, dims, "CIC", 2)
     assert cf0 == 0 and cf1 == 1 and sp1 == 0
     assert per_bin_err(b.Pk, a.Pk).max() <= 1e-5
@@ -80,7 +81,7 @@ def test_overflow_spills_and_falls_back(P, oracle):
     ctx = _native.Context(0)
     dims, n = 128, 2 * 128 ** 3
     uni = synth.uniform(n, BOX, seed=21)
-    spectra(P, ctx, uni, dims, "CIC", 1)                     # learns uniform occupancy
+    spectra(P, ctx, uni, dims, "CIC", 1, sort="exact")       # learns uniform occupancy
     _, (cf, sp) = spectra(P, ctx, uni, dims, "CIC", 1)
     assert cf == 1 and sp == 0
     # the same size and scheme, but a third of the particles in 30 clumps
