@@ -681,6 +681,8 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
                 unsigned *__restrict__ spill_n, unsigned *__restrict__ status) {
     extern __shared__ __align__(16) float sm[];
     constexpr int WS = HAS_W ? KP : 0;
+    constexpr int PT = KP / kPartThreads;   // particles of a chunk per thread
+    static_assert(KP % kPartThreads == 0, "whole chunks per thread");
     float *sp2 = sm + 6 * KP + 2 * WS;                   // 3*KP in key order
     float *sw2 = sp2 + 3 * KP;
     unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + WS);
@@ -745,6 +747,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         mbar_init(&s_bar[1], 1);
         mbar_init_fence();
     }
+    for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;
     __syncthreads();
     unsigned parity = 0u, pend = 0u;
     long long r0;
@@ -802,37 +805,53 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
                 for (int j = threadIdx.x; j < cnt; j += blockDim.x) sw[j] = __ldcs(srcw + r0 + j);
             __syncthreads();
         }
-        for (int k = threadIdx.x; k < nkeys; k += blockDim.x) hist[k] = 0u;
-        __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const float *q = sp + 3 * i;
-            const int t = tile_of<MAS>(q[0], q[1], q[2], inv, g);
-            const int key = FINE ? t - keybase : t / g.F;
-            skey[i] = (unsigned short)key;
-            atomicAdd(&hist[key], 1u);
+        // (hist is zero here: cleared before the loop and in the write-out
+        // of the previous chunk)
+        // each thread's PT particles stay in registers from here to the
+        // counting sort, with their key and their rank within the key (the
+        // histogram atomic's old value)
+        float px[PT], py[PT], pz[PT];
+        int pk[PT];
+        unsigned pr[PT];
+#pragma unroll
+        for (int u = 0; u < PT; ++u) {
+            const int i = threadIdx.x + u * kPartThreads;
+            pk[u] = -1;
+            if (i < cnt) {
+                const float *q = sp + 3 * i;
+                px[u] = q[0];
+                py[u] = q[1];
+                pz[u] = q[2];
+                const int t = tile_of<MAS>(px[u], py[u], pz[u], inv, g);
+                pk[u] = FINE ? t - keybase : t / g.F;
+                pr[u] = atomicAdd(&hist[pk[u]], 1u);
+            }
         }
         __syncthreads();
         const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
-        unsigned my_base = 0u, room = 0u, sb = 0u;
-        if (hv) {
-            my_base = atomicAdd(&cursor[keybase + threadIdx.x], hv);
-            room = my_base >= cap ? 0u : min(hv, cap - my_base);
-            if (hv > room) sb = atomicAdd(spill_n, hv - room);
-        }
+        // reserve the key's run now; its value is first needed after the
+        // counting sort, so the atomic's round trip overlaps the scan and
+        // the sort
+        unsigned my_base = 0u;
+        if (hv) my_base = atomicAdd(&cursor[keybase + threadIdx.x], hv);
         const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
-        if (threadIdx.x < nkeys) hist[threadIdx.x] = ex;   // running cursor of the counting sort
+        if (threadIdx.x < nkeys) hist[threadIdx.x] = ex;   // each key's first position
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const int key = skey[i];
-            const unsigned r = atomicAdd(&hist[key], 1u);
-            const float *q = sp + 3 * i;
-            sp2[3 * r] = q[0];
-            sp2[3 * r + 1] = q[1];
-            sp2[3 * r + 2] = q[2];
-            if (HAS_W) sw2[r] = sw[i];
-            skey2[r] = (unsigned short)key;
+#pragma unroll
+        for (int u = 0; u < PT; ++u) {
+            if (pk[u] >= 0) {
+                const unsigned r = hist[pk[u]] + pr[u];
+                sp2[3 * r] = px[u];
+                sp2[3 * r + 1] = py[u];
+                sp2[3 * r + 2] = pz[u];
+                if (HAS_W) sw2[r] = sw[threadIdx.x + u * kPartThreads];
+                skey2[r] = (unsigned short)pk[u];
+            }
         }
         if (threadIdx.x < nkeys) {
+            const unsigned room = my_base >= cap ? 0u : min(hv, cap - my_base);
+            unsigned sb = 0u;
+            if (hv > room) sb = atomicAdd(spill_n, hv - room);
             // unsigned arithmetic modulo 2^32: every slot and spill index is
             // below 2^32 (the host checks the slot arrays' sizes)
             gdiff[threadIdx.x] = (unsigned)(keybase + threadIdx.x) * cap + my_base - ex;
@@ -840,6 +859,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
             gsp[threadIdx.x] = sb - (ex + room);
         }
         __syncthreads();
+        for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;   // next chunk
         for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
             const int key = skey2[e];
             const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
