@@ -78,5 +78,10 @@ __device__ __forceinline__ bool mbar_wait_parity(uint64_t *bar, unsigned parity)
 // Device status word bits (pyl_ctx::d_status), read back by the host at its
 // next synchronisation point.
 constexpr unsigned kStatusWaitTimeout = 1u;
+// The exact tile sort found particles that its counting pass had not
+// counted where they landed: the positions changed between its passes (a
+// caller still writing them on another stream).  The overflowing particles
+// are dropped, the deposit is skipped, and the call reports an error.
+constexpr unsigned kStatusInputChanged = 2u;
 
 }  // namespace pyl

@@ -10,6 +10,7 @@
 #include <mutex>
 #include <thread>
 
+#include "async_copy.cuh"
 #include "common.cuh"
 
 using pyl::FftPlan;
@@ -36,6 +37,10 @@ int status_check(pyl_ctx *ctx) {
     PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (s) {
         PYL_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof s, ctx->stream));
+        if (s & kStatusInputChanged)
+            return fail(ctx, PYL_ERR_ARG,
+                        "the positions changed while they were sorted (is another stream still "
+                        "writing them? synchronise it first); the result was not computed");
         return fail(ctx, PYL_ERR_TIMEOUT, "a device-side wait gave up (copy not completed)");
     }
     return PYL_OK;
@@ -701,9 +706,14 @@ int finalize(pyl_ctx *ctx, const ModeTables &T, const std::vector<double> &raw,
         if (out->k3D) out->k3D[b - 1] = (T.k3Dsum[b] / N) * kF;
         if (out->Nmodes3D) out->Nmodes3D[b - 1] = N;
         if (out->Pk) {
-            out->Pk[3 * (b - 1) + 0] = (P3[3 * b + 0] * inv_mean2 / N) * unit;
-            out->Pk[3 * (b - 1) + 1] = (P3[3 * b + 1] * inv_mean2 * 5.0 / N) * unit;
-            out->Pk[3 * (b - 1) + 2] = (P3[3 * b + 2] * inv_mean2 * 9.0 / N) * unit;
+            // the device sums the moments S0, S1, S2 of |delta|^2 in mu^2;
+            // the Legendre sums (Pk_library.pyx:362-365) follow from them
+            const double S0 = P3[3 * b + 0], S1 = P3[3 * b + 1], S2 = P3[3 * b + 2];
+            const double L2 = (3.0 * S1 - S0) / 2.0;
+            const double L4 = (35.0 * S2 - 30.0 * S1 + 3.0 * S0) / 8.0;
+            out->Pk[3 * (b - 1) + 0] = (S0 * inv_mean2 / N) * unit;
+            out->Pk[3 * (b - 1) + 1] = (L2 * inv_mean2 * 5.0 / N) * unit;
+            out->Pk[3 * (b - 1) + 2] = (L4 * inv_mean2 * 9.0 / N) * unit;
         }
         if ((what & PYL_PK_PHASE) && out->Pkphase) out->Pkphase[b - 1] = (Pph[b] / N) * unit;
     }

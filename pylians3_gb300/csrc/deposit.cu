@@ -522,6 +522,7 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
     unsigned *loff = hist + kMaxKeys;
     unsigned *lcur = loff + kMaxKeys;
     unsigned *gbase = lcur + kMaxKeys;
+    unsigned *groom = gbase + kMaxKeys;   // elements of the key's run that fit its region
     __shared__ unsigned s_warp[32];
     __shared__ long long s_seg[2];
     __shared__ __align__(8) uint64_t s_bar[2];
@@ -610,7 +611,13 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             for (int i = threadIdx.x; i < cs; i += blockDim.x) {
                 const float *q = sp + 3 * (o + i);
                 const int t = tile_of<MAS>(q[0], q[1], q[2], inv, g);
-                const int key = FINE ? t - keybase : t / g.F;
+                int key = FINE ? t - keybase : t / g.F;
+                if (FINE && (unsigned)key >= (unsigned)nkeys) {
+                    // not of this bucket: a slot the first pass left unwritten
+                    // because the positions changed after the counting pass
+                    atomicOr(status, kStatusInputChanged);
+                    key = 0;
+                }
                 skey[i] = (unsigned short)key;
                 atomicAdd(&hist[key], 1u);
             }
@@ -637,14 +644,26 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
                 if (HAS_W) sw2[r] = sw[o + i];
                 skey2[r] = (unsigned short)key;
             }
-            if (threadIdx.x < nkeys) gbase[threadIdx.x] = my_base;
+            if (threadIdx.x < nkeys) {
+                gbase[threadIdx.x] = my_base;
+                // the key's region ends where the counting pass put the next
+                // one; a run that would cross it (only when the positions
+                // changed between the passes) is cut there and flagged
+                const int kt = keybase + threadIdx.x;
+                const unsigned end = FINE ? start[kt + 1] : start[min((kt + 1) * g.F, g.ntiles)];
+                const unsigned room = my_base >= end ? 0u : min(hv, end - my_base);
+                if (room < hv) atomicOr(status, kStatusInputChanged);
+                groom[threadIdx.x] = room;
+            }
             __syncthreads();
             // key runs are contiguous both here and in the destination; one
             // particle per thread: consecutive threads hold consecutive slots
             // of a run, so each of the three stores covers one span
             for (int e = threadIdx.x; e < cs; e += blockDim.x) {
                 const int key = skey2[e];
-                const size_t d = (size_t)gbase[key] + (e - loff[key]);
+                const unsigned j = (unsigned)e - loff[key];
+                if (j >= groom[key]) continue;
+                const size_t d = (size_t)gbase[key] + j;
                 const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
                 dst[3 * d] = x;
                 dst[3 * d + 1] = y;
@@ -909,7 +928,8 @@ k_scatter_frontier(const float *__restrict__ src, const float *__restrict__ srcw
                    float *__restrict__ dst, float *__restrict__ dstw,
                    const unsigned *__restrict__ mode, unsigned cap,
                    float *__restrict__ spill, float *__restrict__ spillw,
-                   unsigned *__restrict__ spill_n) {
+                   unsigned *__restrict__ spill_n, const unsigned *__restrict__ start,
+                   unsigned *__restrict__ status) {
     if (!cap && *mode != kSortFrontier) return;   // the whole grid takes the same branch
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -928,6 +948,12 @@ k_scatter_frontier(const float *__restrict__ src, const float *__restrict__ srcw
         if (lane == leader) base = atomicAdd(&cursor[t], (unsigned)__popc(peers));
         base = __shfl_sync(peers, base, leader);
         const unsigned r = base + __popc(peers & lt);
+        if (!cap && r >= start[t + 1]) {
+            // beyond the tile's counted region: the positions changed after
+            // the counting pass
+            atomicOr(status, kStatusInputChanged);
+            continue;
+        }
         if (!cap || r < cap) {
             const size_t slot = cap ? (size_t)t * cap + r : (size_t)r;
             dst[3 * slot] = x;
@@ -1051,7 +1077,11 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                const unsigned *__restrict__ start, const uint2 *__restrict__ items,
                const unsigned *__restrict__ nitems, float inv, TileGeom g,
                float *__restrict__ grid, int vec4, float *__restrict__ glo,
-               const unsigned *__restrict__ cap_count, unsigned capT, unsigned ipt) {
+               const unsigned *__restrict__ cap_count, unsigned capT, unsigned ipt,
+               const unsigned *__restrict__ status) {
+    // the sort found that the positions changed under it: its tiles may hold
+    // unwritten slots, so nothing is deposited (the call reports the error)
+    if (*status & kStatusInputChanged) return;
     constexpr bool FIXED = ACC == kAccFixed;
     constexpr bool COMP = ACC == kAccComp;
     // Fewest fractional bits a fixed-point item may keep; an item whose bound
@@ -1457,7 +1487,7 @@ TileGeom make_geom(int dims, int mas) {
 // two input buffers, the key-ordered buffer, keys and per-key tables
 size_t partition_smem(bool weighted) {
     return sizeof(float) * (9 * (size_t)KP + (weighted ? 3 * (size_t)KP : 0)) +
-           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 4 * kMaxKeys;
+           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 5 * kMaxKeys;
 }
 
 // k_partition_cap: the same buffers, four per-key tables and the bucket
@@ -1542,7 +1572,8 @@ int launch_capacity_t(pyl_ctx *ctx, const float *pos, long long n, const float *
             long long blocks = (n + 255) / 256;
             if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
             k_scatter_frontier<MAS, HAS_W><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
-                pos, W, n, inv, g, fcur, b2, w2, nullptr, capT, sp, spw, spill_n);
+                pos, W, n, inv, g, fcur, b2, w2, nullptr, capT, sp, spw, spill_n, nullptr,
+                ctx->d_status);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
         }
@@ -1560,7 +1591,8 @@ int launch_capacity_t(pyl_ctx *ctx, const float *pos, long long n, const float *
         if ((st2 = wait_grid(ctx))) return st2;
         StageScope s(ctx, ST_DEPOSIT);
         kernel<<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(b2, w2, nullptr, nullptr, nullptr, inv,
-                                                           g, grid, vec4, nullptr, fcur, capT, ipt);
+                                                           g, grid, vec4, nullptr, fcur, capT, ipt,
+                                                           ctx->d_status);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         return PYL_OK;
@@ -1681,7 +1713,8 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
             long long blocks = (n + 255) / 256;
             if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
             k_scatter_frontier<MAS, HAS_W><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
-                pos, W, n, inv, g, fcur, b2, w2, mode, 0u, nullptr, nullptr, nullptr);
+                pos, W, n, inv, g, fcur, b2, w2, mode, 0u, nullptr, nullptr, nullptr, start,
+                ctx->d_status);
             ctx->launches++;
             PYL_CUDA(ctx, cudaGetLastError());
         }
@@ -1699,7 +1732,8 @@ int launch_sorted_t(pyl_ctx *ctx, const float *pos, long long n, const float *W,
         if ((st2 = wait_grid(ctx))) return st2;
         StageScope s(ctx, ST_DEPOSIT);
         kernel<<<(unsigned)grid_n, 512, rsm, ctx->stream>>>(b2, w2, start, items, nitems, inv, g,
-                                                           grid, vec4, glo, nullptr, 0u, 1u);
+                                                           grid, vec4, glo, nullptr, 0u, 1u,
+                                                           ctx->d_status);
         ctx->launches++;
         PYL_CUDA(ctx, cudaGetLastError());
         return PYL_OK;

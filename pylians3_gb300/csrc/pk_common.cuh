@@ -81,7 +81,10 @@ __device__ __forceinline__ void mode_extras(Hist &H, const PkAcc &acc, int n2, i
 }
 
 // Runs of consecutive modes of one lane that fall into the same |k| bin:
-// the multipole sums of the current run are kept in registers.  The lane's
+// the sums of the current run are kept in registers.  A bin's three sums
+// are the moments S0 = sum |delta|^2, S1 = sum |delta|^2 mu^2 and S2 = sum
+// |delta|^2 mu^4; the Legendre sums of Pk_library.pyx:362-365 are formed
+// from them in float64 when the spectrum is finalised (finalize).  The lane's
 // first run (head) and its last run (tail) may continue in the neighbouring
 // lanes' modes, so they are kept for the warp merge (warp_flush_runs); the
 // runs in between are complete and go to the shared histogram as they close.
@@ -105,9 +108,10 @@ struct RunAcc {
             cb = b;
             c0 = c1 = c2 = 0.f;
         }
+        const float t = d2 * mu2;
         c0 += d2;
-        c1 += d2 * (3.f * mu2 - 1.f) * 0.5f;
-        c2 += d2 * ((35.f * mu2 - 30.f) * mu2 + 3.f) * 0.125f;
+        c1 += t;
+        c2 = fmaf(t, mu2, c2);
     }
 };
 
@@ -188,20 +192,27 @@ __device__ __forceinline__ void bin_run(RunAcc &R, Hist &H, const PkAcc &acc, co
     int bin = isqrt_dev(kx0 * kx0 + r2);
     if (!plane) {
         const int kpar_c = axis == 1 ? ky : kz;   // kpar when it is not kx
+        // |k|^2 and k_par^2 also in float, exact (< 2^24), from kxx in
+        // float: no integer-to-float conversions per mode
+        const float r2f = (float)r2, kpc2f = (float)(kpar_c * kpar_c);
+        const float kxx0f = (float)kxx0, nf = (float)n;
 #pragma unroll
         for (int i = 0; i < L; ++i) {
             const int kxx = kxx0 + i;
-            const int kx = kxx > mid ? kxx - n : kxx;
+            const bool wrap = kxx > mid;
+            const int kx = wrap ? kxx - n : kxx;
             const int n2 = kx * kx + r2;          // > 0: kz != 0 here
             bin += ((bin + 1) * (bin + 1) <= n2) - (bin * bin > n2);
             const float2 v = ln[pad(kxx)];
-            const int kpar = axis == 0 ? kx : kpar_c;
+            const float kxf = (kxx0f + (float)i) - (wrap ? nf : 0.f);
+            const float n2f = fmaf(kxf, kxf, r2f);
+            const float kpar2f = axis == 0 ? kxf * kxf : kpc2f;
             const float f = win[pad(kxx)] * wyz;
             const float re = v.x * f, im = v.y * f;
             const float d2 = re * re + im * im;
-            const float mu2 = __fdividef((float)(kpar * kpar), (float)n2);
+            const float mu2 = __fdividef(kpar2f, n2f);
             R.add(H, bin, d2, mu2);
-            if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, kpar, re, d2, mid);
+            if (WHAT) mode_extras<WHAT>(H, acc, n2, bin, axis == 0 ? kx : kpar_c, re, d2, mid);
         }
         return;
     }
@@ -279,9 +290,9 @@ __device__ __forceinline__ void bin_mode(BinHist &H, const PkAcc &acc, float2 v,
     const float re = v.x * f, im = v.y * f;
     const float d2 = re * re + im * im;
     const float mu2 = n2 > 0 ? (float)(kpar * kpar) / (float)n2 : 0.f;
-    atomicAdd(&H.h3[3 * bin + 0], d2);
-    atomicAdd(&H.h3[3 * bin + 1], d2 * (3.f * mu2 - 1.f) * 0.5f);
-    atomicAdd(&H.h3[3 * bin + 2], d2 * ((35.f * mu2 - 30.f) * mu2 + 3.f) * 0.125f);
+    atomicAdd(&H.h3[3 * bin + 0], d2);                // moments S0, S1, S2 (see RunAcc)
+    atomicAdd(&H.h3[3 * bin + 1], d2 * mu2);
+    atomicAdd(&H.h3[3 * bin + 2], d2 * mu2 * mu2);
     if (WHAT & PYL_PK_1D) {
         if (n2 <= mid * mid) atomicAdd(&H.h1[abs(kpar)], d2);
     }
