@@ -471,19 +471,24 @@ def run_ours(a):
             P.power_spectrum(host, a.dims, BOX, a.mas, axis=a.axis, ctx=ctx)
         single = max_over_ranks(time.perf_counter() - t0, world, "cuda")
         # the public batched call: each step's positions go host -> device
-        # while the previous step computes (two contexts in flight)
-        P.power_spectra([host] * 2, a.dims, BOX, a.mas, axis=a.axis)
-        barrier()
-        t0 = time.perf_counter()
-        P.power_spectra([host] * a.steps, a.dims, BOX, a.mas, axis=a.axis)
-        t1 = time.perf_counter()
-        sec = max_over_ranks(t1 - t0, world, "cuda")
+        # while the previous step computes (two contexts in flight); warmed
+        # with a full-length pass, then the better of two timed passes
+        P.power_spectra([host] * max(4, a.steps), a.dims, BOX, a.mas, axis=a.axis)
+        passes = []
+        for _ in range(2):
+            barrier()
+            t0 = time.perf_counter()
+            P.power_spectra([host] * a.steps, a.dims, BOX, a.mas, axis=a.axis)
+            passes.append(time.perf_counter() - t0)
+        sec = max_over_ranks(min(passes), world, "cuda")
         kmax = _native.pk_sizes(a.dims)[0]
         e2e = {"value": job_rate(world, a.steps, sec), "unit": UNIT,
                "h2d_bytes_per_step": a.particles * 12,
                "d2h_bytes_per_step": 8 * (5 * (kmax + 1)),
                "ms_per_step": sec / a.steps * 1e3,
-               "api": "pylians3_gb300.power_spectra, pinned host positions, 2 sets in flight",
+               "api": "pylians3_gb300.power_spectra, pinned host positions, 2 sets in flight "
+                      "(the better of two timed passes)",
+               "passes_ms_per_step": [p / a.steps * 1e3 for p in passes],
                "single_call_value": job_rate(world, a.steps, single),
                "single_call_api": "pylians3_gb300.power_spectrum, one call at a time"}
 
@@ -568,6 +573,30 @@ def headline_stream(a, P, host, device_value):
              "api": "MAS_library.MA + numpy delta/mean - 1 + Pk_library.Pk, one request at a "
                     "time, host numpy arrays (Pk_snapshot.py:66-89)"}
 
+    # the same drop-in sequence for a caller whose particles are already on
+    # the device (torch CUDA tensors in and out of MA and Pk)
+    import torch
+    dev_pos = torch.from_numpy(np.asarray(host)).cuda()
+
+    def plain_device_one():
+        delta = torch.zeros((a.dims,) * 3, device="cuda")
+        P.MAS_library.MA(dev_pos, delta, BOX, a.mas)
+        delta /= (a.particles * 1.0 / a.dims ** 3)
+        delta -= 1.0
+        return P.Pk_library.Pk(delta, BOX, axis=a.axis, MAS=a.mas, threads=1, verbose=False)
+
+    plain_device_one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        plain_device_one()
+    torch.cuda.synchronize()
+    t_pd = time.perf_counter() - t0
+    del dev_pos
+    plain_device = {"value": K / t_pd,
+                    "api": "the same drop-in MA + delta/mean - 1 + Pk sequence on torch CUDA "
+                           "tensors (positions already on the device), one request at a time"}
+
     P.power_spectra([host] * 2, a.dims, BOX, a.mas, axis=a.axis)
     t0 = time.perf_counter()
     P.power_spectra([host] * K, a.dims, BOX, a.mas, axis=a.axis)
@@ -606,13 +635,15 @@ def headline_stream(a, P, host, device_value):
     return {
         "stream": "%d requests: %d pinned host particles each -> %d^3 %s spectrum, axis %d"
                   % (K, a.particles, a.dims, a.mas, a.axis),
-        "plain": plain, "batched": batched, "served": served, "served_poisson": poisson,
+        "plain": plain, "plain_device": plain_device,
+        "batched": batched, "served": served, "served_poisson": poisson,
         "device_resident": {"value": device_value,
                             "api": "pyl_pk_particles on device-resident positions (value)"},
         "ratio_served_batched_vs_plain": best / plain["value"],
         "ratio_batched_vs_plain": batched["value"] / plain["value"],
         "ratio_served_vs_plain": served["value"] / plain["value"],
         "ratio_device_resident_vs_plain": device_value / plain["value"],
+        "ratio_device_resident_vs_plain_device": device_value / plain_device["value"],
     }
 
 
