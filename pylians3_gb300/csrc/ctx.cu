@@ -755,6 +755,15 @@ int check_particles(pyl_ctx *ctx, const pyl_pk_request &r) {
 // Issues one particles -> spectrum request on the context stream: upload
 // (host inputs), zero, deposit, the FFT passes and the fused binning, then
 // the raw sums, the k = 0 mode and the mass copied to `dst` (host, pinned).
+// Particle sets uploaded from host memory share one host link: on a device,
+// each upload (from any context) waits for the one issued before it, so that
+// one runs at a time at the link's full rate while the other contexts'
+// requests compute (several uploads at once only share the link and then
+// leave it idle while their requests all compute together).  Not applied
+// while a sequence is captured into a graph (the event lives outside it).
+static std::mutex g_upload_mu;
+static std::map<int, cudaEvent_t> g_upload_ev;   // device -> after its last upload
+
 int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, int flags,
                     void *dst) {
     int st = PYL_OK;
@@ -765,16 +774,28 @@ int issue_particles(pyl_ctx *ctx, const pyl_pk_request &r, const ModeTables &T, 
         StageScope s(ctx, ST_H2D);
         float *p = (float *)ws_get(ctx, "ma_pos", sizeof(float) * (size_t)(3 * n), &st);
         if (!p) return st;
+        float *w = nullptr;
+        if (r.W) {
+            w = (float *)ws_get(ctx, "ma_w", sizeof(float) * (size_t)n, &st);
+            if (!w) return st;
+        }
+        std::unique_lock<std::mutex> lock(g_upload_mu, std::defer_lock);
+        cudaEvent_t *chain = nullptr;
+        if (!ctx->capturing) {
+            lock.lock();
+            chain = &g_upload_ev[ctx->device];
+            if (*chain) PYL_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, *chain, 0));
+            else PYL_CUDA(ctx, cudaEventCreateWithFlags(chain, cudaEventDisableTiming));
+        }
         PYL_CUDA(ctx, cudaMemcpyAsync(p, r.pos, sizeof(float) * (size_t)(3 * n),
                                       cudaMemcpyHostToDevice, ctx->stream));
         dpos = p;
-        if (r.W) {
-            float *w = (float *)ws_get(ctx, "ma_w", sizeof(float) * (size_t)n, &st);
-            if (!w) return st;
+        if (w) {
             PYL_CUDA(ctx, cudaMemcpyAsync(w, r.W, sizeof(float) * (size_t)n,
                                           cudaMemcpyHostToDevice, ctx->stream));
             dW = w;
         }
+        if (chain) PYL_CUDA(ctx, cudaEventRecord(*chain, ctx->stream));
     }
     const size_t rb = sizeof(float) * (size_t)dims * dims * dims;
     float *grid = (float *)ws_get(ctx, "pk_grid", rb, &st);

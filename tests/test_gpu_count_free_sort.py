@@ -6,8 +6,9 @@ the occupancy the exact sort saw, and needs no counting pass.  Checked
 through the public API (sort="exact" forces the counting sort) and
 pyl_ctx_last_sort:
   * on uniform input the count-free sort runs without spilling and gives the
-    exact sort's spectrum to 1e-5 of P0 per bin (the grid differs by float32
-    rounding: tile halos reach it through float reductions in any order);
+    exact sort's spectrum to 1e-5 of P0 per bin up to the Nyquist wavenumber
+    and 1e-4 beyond (the grid differs by float32 rounding: tile halos reach
+    it through float reductions in any order);
   * on a coherent (displaced-lattice) input it takes the one-pass frontier
     form and again matches the exact sort;
   * when a request's tiles hold more than the slots allow (a clustered input
@@ -57,9 +58,14 @@ def test_uniform_count_free_equals_exact(P, MAS, weighted):
     assert cf0 == 0 and cf1 == 1 and cf2 == 1 and sp1 == 0 and sp2 == 0
     assert np.array_equal(a.Nmodes3D, b.Nmodes3D)
     # the tiles' halos reach the grid through float reductions in any order
-    # (in both sorts): float32 rounding of the grid, ~1e-7 of P0
-    assert per_bin_err(b.Pk, a.Pk).max() <= 1e-5
-    assert per_bin_err(c.Pk, a.Pk).max() <= 1e-5
+    # (in both sorts), and dense PCS tiles accumulate in float atomics:
+    # float32 rounding of the grid, ~1e-7 of P0 up to the Nyquist wavenumber;
+    # beyond it the PCS deconvolution amplifies it in bins of a few modes
+    mid = dims // 2
+    for x in (b, c):
+        e = per_bin_err(x.Pk, a.Pk)
+        assert e[:mid].max() <= 1e-5
+        assert e.max() <= TOL_PK
     ctx.close()
 
 
