@@ -1237,17 +1237,22 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 // quantized taps -- also goes to its largest tap, so that the
                 // many tiny outer taps rounding to zero cannot bias the mass.
                 if (MIN_BITS >= 20 || !exact_mass) {
+                    // the scale (a power of two) folded into the x weights:
+                    // the same products, exactly, with NT^3 fewer multiplies
+                    float wxs[NT];
+#pragma unroll
+                    for (int l = 0; l < NT; ++l) wxs[l] = wx[l] * scale;
 #pragma unroll
                     for (int l = 0; l < NT; ++l)
 #pragma unroll
                         for (int m = 0; m < NT; ++m) {
-                            const float wxy = wx[l] * wy[m];
+                            const float wxy = wxs[l] * wy[m];
                             const int row = (lx[l] * RY + ly[m]) * RZ;
 #pragma unroll
                             for (int q = 0; q < NT; ++q) {
                                 float v = wxy * wz[q];
                                 if (HAS_W) v *= wt;
-                                atomicAdd(s_int + row + lz[q], __float2int_rn(v * scale));
+                                atomicAdd(s_int + row + lz[q], __float2int_rn(v));
                             }
                         }
                     return;
