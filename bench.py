@@ -442,9 +442,11 @@ def run_ours(a):
             row["frac_moved"] = moved / (ms_st / 1e3) / 1e9 / peak
         stages[name] = row
     traffic = None
-    if all(tr_tab.get((k, key)) for k in ("tile_count", "partition", "deposit", "fft_z", "fft_y",
-                                           "pk_x")):
-        traffic = sum(v for (st, wk), v in tr_tab.items() if wk == key)
+    # whole-spectrum traffic from the committed per-stage figures, when they
+    # cover every stage this run timed
+    timed = [k for k, v in stages.items() if v["moved_bytes"]]
+    if timed and all(tr_tab.get((k, key)) for k in timed):
+        traffic = sum(tr_tab[(k, key)] for k in timed)
     one_pass = a.particles * 12 + 8 * a.dims ** 3
     roof = {"bound": "hbm", "kernel": "one spectrum (all kernels of a step)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
