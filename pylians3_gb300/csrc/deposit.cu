@@ -269,6 +269,7 @@ struct TileGeom {
     int RX, RY, RZ;      // shared footprint extent = T + LO + HI
     int ntiles;
     int F;               // tiles per coarse bucket (power of two)
+    int sF;              // log2 F
     int ncoarse;         // coarse buckets = ceil(ntiles / F)
 };
 
@@ -611,7 +612,7 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
             for (int i = threadIdx.x; i < cs; i += blockDim.x) {
                 const float *q = sp + 3 * (o + i);
                 const int t = tile_of<MAS>(q[0], q[1], q[2], inv, g);
-                int key = FINE ? t - keybase : t / g.F;
+                int key = FINE ? t - keybase : t >> g.sF;
                 if (FINE && (unsigned)key >= (unsigned)nkeys) {
                     // not of this bucket: a slot the first pass left unwritten
                     // because the positions changed after the counting pass
@@ -702,6 +703,9 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
     constexpr int WS = HAS_W ? KP : 0;
     constexpr int PT = KP / kPartThreads;   // particles of a chunk per thread
     static_assert(KP % kPartThreads == 0, "whole chunks per thread");
+    static_assert(PT % 4 == 0, "four particles per group of three 16-byte loads");
+    static_assert(kMaxKeys % 128 == 0 && kMaxKeys <= kPartThreads,
+                  "the one-warp scan reads whole uint4 groups; one key per thread");
     float *sp2 = sm + 6 * KP + 2 * WS;                   // 3*KP in key order
     float *sw2 = sp2 + 3 * KP;
     unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + WS);
@@ -710,7 +714,8 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
     unsigned *gdiff = hist + kMaxKeys;   // slot of key-ordered element e: gdiff[key] + e
     unsigned *glim = gdiff + kMaxKeys;   // elements e < glim[key] fit their slots
     unsigned *gsp = glim + kMaxKeys;     // spill index of the others: gsp[key] + e
-    unsigned *cpre = gsp + kMaxKeys;                     // kMaxKeys + 1 (fine pass)
+    unsigned *hex = gsp + kMaxKeys;      // each key's first position in key order
+    unsigned *cpre = hex + kMaxKeys;                     // kMaxKeys + 1 (fine pass)
     __shared__ unsigned s_warp[32];
     __shared__ __align__(8) uint64_t s_bar[2];
     __shared__ long long s_r0[2];        // fine pass: the next chunk's mapping, by
@@ -776,6 +781,27 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         if (threadIdx.x == 0) issue(r0, 0);
         pend |= 1u;
     }
+    // a chunk's key-ordered particles -> their slots (or the spill list)
+    auto write_out = [&](int wcnt) {
+        for (int e = threadIdx.x; e < wcnt; e += blockDim.x) {
+            const int key = skey2[e];
+            const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
+            if ((unsigned)e < glim[key]) {
+                const size_t d = gdiff[key] + (unsigned)e;
+                dst[3 * d] = x;
+                dst[3 * d + 1] = y;
+                dst[3 * d + 2] = z;
+                if (HAS_W) dstw[d] = sw2[e];
+            } else {
+                const size_t d = gsp[key] + (unsigned)e;
+                spill[3 * d] = x;
+                spill[3 * d + 1] = y;
+                spill[3 * d + 2] = z;
+                if (HAS_W) spillw[d] = sw2[e];
+            }
+        }
+    };
+    int prev_cnt = 0;   // particles of the previous chunk still to be written
     int b = 0;
     for (; c < nchunks; c += gridDim.x, b ^= 1) {
         const long long cn = c + gridDim.x;
@@ -824,50 +850,103 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
                 for (int j = threadIdx.x; j < cnt; j += blockDim.x) sw[j] = __ldcs(srcw + r0 + j);
             __syncthreads();
         }
-        // (hist is zero here: cleared before the loop and in the write-out
-        // of the previous chunk)
+        // (hist is zero here: cleared before the loop and after the
+        // previous chunk's scan)
         // each thread's PT particles stay in registers from here to the
         // counting sort, with their key and their rank within the key (the
         // histogram atomic's old value)
-        float px[PT], py[PT], pz[PT];
+        // (thread j takes the PT consecutive particles from PT * j: four
+        // particles are three aligned 16-byte shared loads)
+        // (weights too: the next bulk copy into this buffer may be issued
+        // before the sort below is done)
+        float px[PT], py[PT], pz[PT], pw[HAS_W ? PT : 1];
         int pk[PT];
         unsigned pr[PT];
 #pragma unroll
-        for (int u = 0; u < PT; ++u) {
-            const int i = threadIdx.x + u * kPartThreads;
-            pk[u] = -1;
-            if (i < cnt) {
-                const float *q = sp + 3 * i;
-                px[u] = q[0];
-                py[u] = q[1];
-                pz[u] = q[2];
-                const int t = tile_of<MAS>(px[u], py[u], pz[u], inv, g);
-                pk[u] = FINE ? t - keybase : t / g.F;
-                pr[u] = atomicAdd(&hist[pk[u]], 1u);
+        for (int q4 = 0; q4 < PT / 4; ++q4) {
+            const int i0 = PT * threadIdx.x + 4 * q4;
+            const float4 *q = reinterpret_cast<const float4 *>(sp + 3 * i0);
+            const float4 a = q[0], b4 = q[1], c4 = q[2];
+            const float xs[4] = {a.x, a.w, b4.z, c4.y};
+            const float ys[4] = {a.y, b4.x, b4.w, c4.z};
+            const float zs[4] = {a.z, b4.y, c4.x, c4.w};
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const int u = 4 * q4 + v;
+                pk[u] = -1;
+                if (i0 + v < cnt) {
+                    px[u] = xs[v];
+                    py[u] = ys[v];
+                    pz[u] = zs[v];
+                    if (HAS_W) pw[u] = sw[i0 + v];
+                    const int t = tile_of<MAS>(px[u], py[u], pz[u], inv, g);
+                    pk[u] = FINE ? t - keybase : t >> g.sF;
+                    pr[u] = atomicAdd(&hist[pk[u]], 1u);
+                }
             }
         }
         __syncthreads();
         const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
         // reserve the key's run now; its value is first needed after the
-        // counting sort, so the atomic's round trip overlaps the scan and
-        // the sort
+        // counting sort, so the atomic's round trip overlaps the previous
+        // chunk's write-out, the scan and the sort
         unsigned my_base = 0u;
         if (hv) my_base = atomicAdd(&cursor[keybase + threadIdx.x], hv);
-        const unsigned ex = block_exclusive_scan(hv, s_warp, nullptr);
-        if (threadIdx.x < nkeys) hist[threadIdx.x] = ex;   // each key's first position
+        if (prev_cnt > 0) write_out(prev_cnt);
+        if (threadIdx.x < 32) {
+            // one warp scans the key counts (KPL consecutive keys per lane):
+            // each key's first position in key order -> hex
+            constexpr int KPL = kMaxKeys / 32;
+            const int lane = threadIdx.x;
+            unsigned cv[KPL], sum = 0u;
+#pragma unroll
+            for (int j = 0; j < KPL; j += 4) {
+                const uint4 h4 = *reinterpret_cast<const uint4 *>(hist + lane * KPL + j);
+                cv[j] = h4.x;
+                cv[j + 1] = h4.y;
+                cv[j + 2] = h4.z;
+                cv[j + 3] = h4.w;
+            }
+#pragma unroll
+            for (int j = 0; j < KPL; ++j) sum += cv[j];
+            unsigned incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            unsigned run = incl - sum;
+#pragma unroll
+            for (int j = 0; j < KPL; j += 4) {
+                uint4 e4;
+                e4.x = run;
+                run += cv[j];
+                e4.y = run;
+                run += cv[j + 1];
+                e4.z = run;
+                run += cv[j + 2];
+                e4.w = run;
+                run += cv[j + 3];
+                *reinterpret_cast<uint4 *>(hex + lane * KPL + j) = e4;
+            }
+        }
         __syncthreads();
+        // every read of this chunk's histogram and of the previous chunk's
+        // key-ordered buffer and tables is behind the barrier
+        for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;   // next chunk
 #pragma unroll
         for (int u = 0; u < PT; ++u) {
             if (pk[u] >= 0) {
-                const unsigned r = hist[pk[u]] + pr[u];
+                const unsigned r = hex[pk[u]] + pr[u];
                 sp2[3 * r] = px[u];
                 sp2[3 * r + 1] = py[u];
                 sp2[3 * r + 2] = pz[u];
-                if (HAS_W) sw2[r] = sw[threadIdx.x + u * kPartThreads];
+                if (HAS_W) sw2[r] = pw[u];
                 skey2[r] = (unsigned short)pk[u];
             }
         }
         if (threadIdx.x < nkeys) {
+            const unsigned ex = hex[threadIdx.x];
             const unsigned room = my_base >= cap ? 0u : min(hv, cap - my_base);
             unsigned sb = 0u;
             if (hv > room) sb = atomicAdd(spill_n, hv - room);
@@ -877,29 +956,13 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
             glim[threadIdx.x] = ex + room;
             gsp[threadIdx.x] = sb - (ex + room);
         }
-        __syncthreads();
-        for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;   // next chunk
-        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-            const int key = skey2[e];
-            const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
-            if ((unsigned)e < glim[key]) {
-                const size_t d = gdiff[key] + (unsigned)e;
-                dst[3 * d] = x;
-                dst[3 * d + 1] = y;
-                dst[3 * d + 2] = z;
-                if (HAS_W) dstw[d] = sw2[e];
-            } else {
-                const size_t d = gsp[key] + (unsigned)e;
-                spill[3 * d] = x;
-                spill[3 * d + 1] = y;
-                spill[3 * d + 2] = z;
-                if (HAS_W) spillw[d] = sw2[e];
-            }
-        }
-        __syncthreads();
+        // this chunk is written out during the next one (after its key
+        // phase and barrier), or after the loop
+        prev_cnt = cnt;
         if (FINE && cn < nchunks) {
-            // thread 0's mapping of the next chunk; a copy is in flight for
-            // it when it is a whole chunk
+            // thread 0's mapping of the next chunk (written before this
+            // chunk's barriers); a copy is in flight for it when it is a
+            // whole chunk
             nr0 = s_r0[b ^ 1];
             ncnt = s_ck[b ^ 1][0];
             nkb = s_ck[b ^ 1][1];
@@ -911,6 +974,8 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         keybase = nkb;
         nkeys = nnk;
     }
+    __syncthreads();
+    if (prev_cnt > 0) write_out(prev_cnt);
 }
 
 // Single-pass alternative to the two partition passes: every particle takes
@@ -1433,6 +1498,7 @@ void finish_geom(TileGeom &g, int dims, int mas, int F) {
         while ((g.ntiles + g.F - 1) / g.F > kMaxKeys) g.F *= 2;
         if (g.F > kMaxKeys) g.F = kMaxKeys;
     }
+    g.sF = ilog2_ceil(g.F);
     g.ncoarse = (g.ntiles + g.F - 1) / g.F;
 }
 
@@ -1485,6 +1551,7 @@ TileGeom make_geom(int dims, int mas) {
     while ((long long)g.F * g.F < g.ntiles) g.F *= 2;
     while ((g.ntiles + g.F - 1) / g.F > kMaxKeys) g.F *= 2;
     if (g.F > kMaxKeys) g.F = kMaxKeys;
+    g.sF = lg(g.F);
     g.ncoarse = (g.ntiles + g.F - 1) / g.F;
     return g;
 }
@@ -1495,11 +1562,11 @@ size_t partition_smem(bool weighted) {
            sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 5 * kMaxKeys;
 }
 
-// k_partition_cap: the same buffers, four per-key tables and the bucket
+// k_partition_cap: the same buffers, five per-key tables and the bucket
 // chunk prefix
 size_t partition_cap_smem(bool weighted) {
     return sizeof(float) * (9 * (size_t)KP + (weighted ? 3 * (size_t)KP : 0)) +
-           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (5 * kMaxKeys + 1);
+           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (6 * kMaxKeys + 1);
 }
 
 unsigned round_up4(double v) {
