@@ -271,7 +271,14 @@ struct TileGeom {
     int F;               // tiles per coarse bucket (power of two)
     int sF;              // log2 F
     int ncoarse;         // coarse buckets = ceil(ntiles / F)
+    int dmask;           // dims - 1 when dims is a power of two, else -1
 };
+
+// Periodic wrap of a cell index: for a power-of-two grid one mask (equal to
+// wrap_idx for every int), else wrap_idx's in-box test and remainder.
+__device__ __forceinline__ int wrap_cell(int i, const TileGeom &g) {
+    return g.dmask >= 0 ? (i & g.dmask) : wrap_idx(i, g.dims);
+}
 
 // Partition shape (compile-time; the defaults are the measured best):
 // particles staged per chunk, threads per CTA (>= kMaxKeys: one scan value
@@ -296,9 +303,9 @@ constexpr unsigned kItemCap = 65536;  // particles per deposit work item
 
 template <int MAS>
 __device__ __forceinline__ int tile_of(float x, float y, float z, float inv, const TileGeom &g) {
-    const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
-    const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
-    const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
+    const int hx = wrap_cell(home_cell<MAS>(cell_dist(x, inv)), g);
+    const int hy = wrap_cell(home_cell<MAS>(cell_dist(y, inv)), g);
+    const int hz = wrap_cell(home_cell<MAS>(cell_dist(z, inv)), g);
     return ((hx >> g.sx) * g.nty + (hy >> g.sy)) * g.ntz + (hz >> g.sz);
 }
 
@@ -785,7 +792,19 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         pend |= 1u;
     }
     // a chunk's key-ordered particles -> their slots (or the spill list)
-    auto write_out = [&](int wcnt) {
+    auto write_out = [&](int wcnt, bool spilled) {
+        if (!spilled) {
+            // every run fits its slots (the common case)
+            for (int e = threadIdx.x; e < wcnt; e += blockDim.x) {
+                const int key = skey2[e];
+                const size_t d = gdiff[key] + (unsigned)e;
+                dst[3 * d] = sp2[3 * e];
+                dst[3 * d + 1] = sp2[3 * e + 1];
+                dst[3 * d + 2] = sp2[3 * e + 2];
+                if (HAS_W) dstw[d] = sw2[e];
+            }
+            return;
+        }
         for (int e = threadIdx.x; e < wcnt; e += blockDim.x) {
             const int key = skey2[e];
             const float x = sp2[3 * e], y = sp2[3 * e + 1], z = sp2[3 * e + 2];
@@ -805,6 +824,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         }
     };
     int prev_cnt = 0;   // particles of the previous chunk still to be written
+    int my_spill = 0;   // this thread's key of that chunk overflowed its slots
     int b = 0;
     for (; c < nchunks; c += gridDim.x, b ^= 1) {
         const long long cn = c + gridDim.x;
@@ -865,37 +885,45 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         float px[PT], py[PT], pz[PT], pw[HAS_W ? PT : 1];
         int pk[PT];
         unsigned pr[PT];
+        // (a whole chunk, the common case, takes the loop without the
+        // per-particle bounds test)
+        auto key_phase = [&](auto whole) {
 #pragma unroll
-        for (int q4 = 0; q4 < PT / 4; ++q4) {
-            const int i0 = PT * threadIdx.x + 4 * q4;
-            const float4 *q = reinterpret_cast<const float4 *>(sp + 3 * i0);
-            const float4 a = q[0], b4 = q[1], c4 = q[2];
-            const float xs[4] = {a.x, a.w, b4.z, c4.y};
-            const float ys[4] = {a.y, b4.x, b4.w, c4.z};
-            const float zs[4] = {a.z, b4.y, c4.x, c4.w};
+            for (int q4 = 0; q4 < PT / 4; ++q4) {
+                const int i0 = PT * threadIdx.x + 4 * q4;
+                const float4 *q = reinterpret_cast<const float4 *>(sp + 3 * i0);
+                const float4 a = q[0], b4 = q[1], c4 = q[2];
+                const float xs[4] = {a.x, a.w, b4.z, c4.y};
+                const float ys[4] = {a.y, b4.x, b4.w, c4.z};
+                const float zs[4] = {a.z, b4.y, c4.x, c4.w};
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const int u = 4 * q4 + v;
-                pk[u] = -1;
-                if (i0 + v < cnt) {
-                    px[u] = xs[v];
-                    py[u] = ys[v];
-                    pz[u] = zs[v];
-                    if (HAS_W) pw[u] = sw[i0 + v];
-                    const int t = tile_of<MAS>(px[u], py[u], pz[u], inv, g);
-                    pk[u] = FINE ? t - keybase : t >> g.sF;
-                    pr[u] = atomicAdd(&hist[pk[u]], 1u);
+                for (int v = 0; v < 4; ++v) {
+                    const int u = 4 * q4 + v;
+                    pk[u] = -1;
+                    if (decltype(whole)::value || i0 + v < cnt) {
+                        px[u] = xs[v];
+                        py[u] = ys[v];
+                        pz[u] = zs[v];
+                        if (HAS_W) pw[u] = sw[i0 + v];
+                        const int t = tile_of<MAS>(px[u], py[u], pz[u], inv, g);
+                        pk[u] = FINE ? t - keybase : t >> g.sF;
+                        pr[u] = atomicAdd(&hist[pk[u]], 1u);
+                    }
                 }
             }
-        }
-        __syncthreads();
+        };
+        if (cnt == KP) key_phase(std::true_type());
+        else key_phase(std::false_type());
+        // (the barrier also tells whether any run of the previous chunk
+        // overflowed its slots)
+        const bool spilled = __syncthreads_or(my_spill) != 0;
         const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
         // reserve the key's run now; its value is first needed after the
         // counting sort, so the atomic's round trip overlaps the previous
         // chunk's write-out, the scan and the sort
         unsigned my_base = 0u;
         if (hv) my_base = atomicAdd(&cursor[keybase + threadIdx.x], hv);
-        if (prev_cnt > 0) write_out(prev_cnt);
+        if (prev_cnt > 0) write_out(prev_cnt, spilled);
         if (threadIdx.x < 32) {
             // one warp scans the key counts (KPL consecutive keys per lane):
             // each key's first position in key order -> hex
@@ -948,11 +976,13 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
                 skey2[r] = (unsigned short)pk[u];
             }
         }
+        my_spill = 0;
         if (threadIdx.x < nkeys) {
             const unsigned ex = hex[threadIdx.x];
             const unsigned room = my_base >= cap ? 0u : min(hv, cap - my_base);
             unsigned sb = 0u;
             if (hv > room) sb = atomicAdd(spill_n, hv - room);
+            my_spill = hv > room;
             // unsigned arithmetic modulo 2^32: every slot and spill index is
             // below 2^32 (the host checks the slot arrays' sizes)
             gdiff[threadIdx.x] = (unsigned)(keybase + threadIdx.x) * cap + my_base - ex;
@@ -977,8 +1007,8 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         keybase = nkb;
         nkeys = nnk;
     }
-    __syncthreads();
-    if (prev_cnt > 0) write_out(prev_cnt);
+    const bool spilled = __syncthreads_or(my_spill) != 0;
+    if (prev_cnt > 0) write_out(prev_cnt, spilled);
 }
 
 // Single-pass alternative to the two partition passes: every particle takes
@@ -1201,9 +1231,9 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             int lmi = 0;       // largest count this thread has seen
             float lmf = 0.f;   // ... or largest sum of |W| (a NaN sticks)
             auto occupy = [&](float x, float y, float z, float w) {
-                const int hx = wrap_idx(home_cell<MAS>(cell_dist(x, inv)), g.dims);
-                const int hy = wrap_idx(home_cell<MAS>(cell_dist(y, inv)), g.dims);
-                const int hz = wrap_idx(home_cell<MAS>(cell_dist(z, inv)), g.dims);
+                const int hx = wrap_cell(home_cell<MAS>(cell_dist(x, inv)), g);
+                const int hy = wrap_cell(home_cell<MAS>(cell_dist(y, inv)), g);
+                const int hz = wrap_cell(home_cell<MAS>(cell_dist(z, inv)), g);
                 const int c = ((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ + (hz - oz + S::LO);
                 if (HAS_W) {
                     const float o = atomicAdd(&s_reg[c], fabsf(w)) + fabsf(w);
@@ -1274,7 +1304,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             {
                 const float d = cell_dist(px, inv);
                 const int c = home_cell<MAS>(d);
-                const int base = wrap_idx(c, g.dims) - ox + S::LO;
+                const int base = wrap_cell(c, g) - ox + S::LO;
                 int o[NT];
                 axis_stencil<MAS>(d, c, o, wx);
 #pragma unroll
@@ -1283,7 +1313,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             {
                 const float d = cell_dist(py, inv);
                 const int c = home_cell<MAS>(d);
-                const int base = wrap_idx(c, g.dims) - oy + S::LO;
+                const int base = wrap_cell(c, g) - oy + S::LO;
                 int o[NT];
                 axis_stencil<MAS>(d, c, o, wy);
 #pragma unroll
@@ -1292,7 +1322,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             {
                 const float d = cell_dist(pz, inv);
                 const int c = home_cell<MAS>(d);
-                const int base = wrap_idx(c, g.dims) - oz + S::LO;
+                const int base = wrap_cell(c, g) - oz + S::LO;
                 int o[NT];
                 axis_stencil<MAS>(d, c, o, wz);
 #pragma unroll
@@ -1503,6 +1533,7 @@ void finish_geom(TileGeom &g, int dims, int mas, int F) {
     }
     g.sF = ilog2_ceil(g.F);
     g.ncoarse = (g.ntiles + g.F - 1) / g.F;
+    g.dmask = (dims & (dims - 1)) == 0 ? dims - 1 : -1;
 }
 
 bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
@@ -1556,6 +1587,7 @@ TileGeom make_geom(int dims, int mas) {
     if (g.F > kMaxKeys) g.F = kMaxKeys;
     g.sF = lg(g.F);
     g.ncoarse = (g.ntiles + g.F - 1) / g.F;
+    g.dmask = (dims & (dims - 1)) == 0 ? dims - 1 : -1;
     return g;
 }
 
