@@ -83,5 +83,8 @@ constexpr unsigned kStatusWaitTimeout = 1u;
 // caller still writing them on another stream).  The overflowing particles
 // are dropped, the deposit is skipped, and the call reports an error.
 constexpr unsigned kStatusInputChanged = 2u;
+// A kernel met a bound its launch should have ruled out (a sort's chunk
+// table): it wrote nothing, the deposit is skipped and the call fails.
+constexpr unsigned kStatusInternal = 4u;
 
 }  // namespace pyl

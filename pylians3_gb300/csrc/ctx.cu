@@ -37,6 +37,9 @@ int status_check(pyl_ctx *ctx) {
     PYL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (s) {
         PYL_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof s, ctx->stream));
+        if (s & kStatusInternal)
+            return fail(ctx, PYL_ERR_UNSUPPORTED, "a sort kernel met a bound its launch excludes; "
+                                               "the result was not computed");
         if (s & kStatusInputChanged)
             return fail(ctx, PYL_ERR_ARG,
                         "the positions changed while they were sorted (is another stream still "

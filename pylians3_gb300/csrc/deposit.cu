@@ -299,6 +299,7 @@ constexpr int KP = PYL_PART_KP;
 constexpr int kPartThreads = PYL_PART_THREADS;
 static_assert(KP % 4 == 0, "bulk copies move whole 16-byte groups");
 constexpr int kMaxKeys = 256;     // buckets of one partition step
+constexpr int kChunkTab = 8192;   // fine partition: chunks per CTA it can map
 constexpr unsigned kItemCap = 65536;  // particles per deposit work item
 
 template <int MAS>
@@ -726,10 +727,11 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
     unsigned *gsp = glim + kMaxKeys;     // spill index of the others: gsp[key] + e
     unsigned *hex = gsp + kMaxKeys;      // each key's first position in key order
     unsigned *cpre = hex + kMaxKeys;                     // kMaxKeys + 1 (fine pass)
+    unsigned *mcnt = cpre + kMaxKeys + 1;    // fine pass: particles of each bucket
+    // fine pass: bucket of this CTA's k-th chunk (blockIdx.x + k * gridDim.x)
+    unsigned char *ctab = reinterpret_cast<unsigned char *>(mcnt + kMaxKeys);
     __shared__ unsigned s_warp[32];
     __shared__ __align__(8) uint64_t s_bar[2];
-    __shared__ long long s_r0[2];        // fine pass: the next chunk's mapping, by
-    __shared__ int s_ck[2][3];           // buffer (written by thread 0)
 
     // chunks: the input in KP pieces (coarse), or each bucket's particles in
     // KP pieces (fine; cpre = exclusive prefix of the chunks per bucket)
@@ -739,26 +741,44 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         const unsigned cnt = c < g.ncoarse ? min(count_in[c], cap_in) : 0u;
         unsigned tot = 0;
         const unsigned ex = block_exclusive_scan((cnt + KP - 1) / KP, s_warp, &tot);
-        if (c < g.ncoarse) cpre[c] = ex;
+        if (c < g.ncoarse) {
+            cpre[c] = ex;
+            mcnt[c] = cnt;
+        }
         if (c == 0) cpre[g.ncoarse] = tot;
         __syncthreads();
         nchunks = tot;
-    } else {
-        nchunks = (n + KP - 1) / KP;
-    }
-    long long c = blockIdx.x;
-    if (c >= nchunks) return;
-    // chunk v -> first particle, count, key base and key count
-    auto map_chunk = [&](long long v, long long &r0, int &cnt, int &keybase, int &nkeys) {
-        if (FINE) {
+        // every chunk of this CTA mapped to its bucket up front, in parallel
+        // (a binary search over the chunk prefix each), so that no thread
+        // waits on one thread's search between chunks
+        if ((long long)blockIdx.x < nchunks &&
+            (nchunks - blockIdx.x + gridDim.x - 1) / gridDim.x > kChunkTab) {
+            // (the host sizes the grid for the table: this does not happen)
+            if (threadIdx.x == 0) atomicOr(status, kStatusInternal);
+            return;
+        }
+        for (int k = threadIdx.x; k < kChunkTab; k += blockDim.x) {
+            const long long v = blockIdx.x + (long long)k * gridDim.x;
+            if (v >= nchunks) break;
             int lo = 0, hi = g.ncoarse - 1;            // last bucket b with cpre[b] <= v
             while (lo < hi) {
                 const int mid = (lo + hi + 1) / 2;
                 if ((long long)cpre[mid] <= v) lo = mid;
                 else hi = mid - 1;
             }
+            ctab[k] = (unsigned char)lo;
+        }
+    } else {
+        nchunks = (n + KP - 1) / KP;
+    }
+    long long c = blockIdx.x;
+    if (c >= nchunks) return;
+    // chunk v (this CTA's kk-th) -> first particle, count, key base and key count
+    auto map_chunk = [&](long long v, int kk, long long &r0, int &cnt, int &keybase, int &nkeys) {
+        if (FINE) {
+            const int lo = ctab[kk];
             const long long k = v - cpre[lo];
-            const long long m = min(count_in[lo], cap_in);
+            const long long m = mcnt[lo];
             r0 = (long long)lo * cap_in + k * KP;
             cnt = (int)min((long long)KP, m - k * KP);
             keybase = lo * g.F;
@@ -782,11 +802,11 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         mbar_init_fence();
     }
     for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;
-    __syncthreads();
+    __syncthreads();   // (also publishes the fine pass's chunk table)
     unsigned parity = 0u, pend = 0u;
     long long r0;
     int cnt, keybase, nkeys;
-    map_chunk(c, r0, cnt, keybase, nkeys);
+    map_chunk(c, 0, r0, cnt, keybase, nkeys);
     if (bulk && cnt == KP) {
         if (threadIdx.x == 0) issue(r0, 0);
         pend |= 1u;
@@ -825,33 +845,16 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
     };
     int prev_cnt = 0;   // particles of the previous chunk still to be written
     int my_spill = 0;   // this thread's key of that chunk overflowed its slots
-    int b = 0;
-    for (; c < nchunks; c += gridDim.x, b ^= 1) {
+    int b = 0, kk = 0;
+    for (; c < nchunks; c += gridDim.x, b ^= 1, ++kk) {
         const long long cn = c + gridDim.x;
         long long nr0 = 0;
         int ncnt = 0, nkb = 0, nnk = 0;
         if (cn < nchunks) {
-            if (FINE) {
-                // one thread maps the next chunk (a binary search over the
-                // buckets) and passes it on through shared memory, read
-                // after this chunk's last barrier
-                if (threadIdx.x == 0) {
-                    map_chunk(cn, nr0, ncnt, nkb, nnk);
-                    s_r0[b ^ 1] = nr0;
-                    s_ck[b ^ 1][0] = ncnt;
-                    s_ck[b ^ 1][1] = nkb;
-                    s_ck[b ^ 1][2] = nnk;
-                    if (bulk && ncnt == KP) {
-                        issue(nr0, b ^ 1);
-                        pend |= 2u >> b;   // the others learn of it after the barrier
-                    }
-                }
-            } else {
-                map_chunk(cn, nr0, ncnt, nkb, nnk);
-                if (bulk && ncnt == KP) {
-                    if (threadIdx.x == 0) issue(nr0, b ^ 1);
-                    pend |= 2u >> b;
-                }
+            map_chunk(cn, kk + 1, nr0, ncnt, nkb, nnk);
+            if (bulk && ncnt == KP) {
+                if (threadIdx.x == 0) issue(nr0, b ^ 1);
+                pend |= 2u >> b;
             }
         }
         float *sp = sm + 3 * KP * b;
@@ -992,16 +995,6 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         // this chunk is written out during the next one (after its key
         // phase and barrier), or after the loop
         prev_cnt = cnt;
-        if (FINE && cn < nchunks) {
-            // thread 0's mapping of the next chunk (written before this
-            // chunk's barriers); a copy is in flight for it when it is a
-            // whole chunk
-            nr0 = s_r0[b ^ 1];
-            ncnt = s_ck[b ^ 1][0];
-            nkb = s_ck[b ^ 1][1];
-            nnk = s_ck[b ^ 1][2];
-            if (bulk && ncnt == KP) pend |= 2u >> b;
-        }
         r0 = nr0;
         cnt = ncnt;
         keybase = nkb;
@@ -1179,7 +1172,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                const unsigned *__restrict__ status) {
     // the sort found that the positions changed under it: its tiles may hold
     // unwritten slots, so nothing is deposited (the call reports the error)
-    if (*status & kStatusInputChanged) return;
+    if (*status & (kStatusInputChanged | kStatusInternal)) return;
     constexpr bool FIXED = ACC == kAccFixed;
     constexpr bool COMP = ACC == kAccComp;
     // Fewest fractional bits a fixed-point item may keep; an item whose bound
@@ -1597,11 +1590,12 @@ size_t partition_smem(bool weighted) {
            sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 5 * kMaxKeys;
 }
 
-// k_partition_cap: the same buffers, five per-key tables and the bucket
-// chunk prefix
+// k_partition_cap: the same buffers, five per-key tables, the bucket chunk
+// prefix and counts and the fine pass's chunk -> bucket table
 size_t partition_cap_smem(bool weighted) {
     return sizeof(float) * (9 * (size_t)KP + (weighted ? 3 * (size_t)KP : 0)) +
-           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (6 * kMaxKeys + 1);
+           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (7 * kMaxKeys + 1) +
+           kChunkTab;
 }
 
 unsigned round_up4(double v) {
@@ -1664,6 +1658,10 @@ int launch_capacity_t(pyl_ctx *ctx, const float *pos, long long n, const float *
             }
             const unsigned nblk = (unsigned)std::min<long long>((n + KP - 1) / KP,
                                                                 (long long)per_sm * sms);
+            // the fine pass maps at most kChunkTab chunks per CTA: it has at
+            // most n / KP + ncoarse chunks (every bucket's last one partial)
+            if ((n / KP + g.ncoarse + 1 + nblk - 1) / nblk > kChunkTab)
+                return fail(ctx, PYL_ERR_UNSUPPORTED, "too many particles for the count-free sort");
             const int bulk_in = ((uintptr_t)pos & 15) == 0 && (!W || ((uintptr_t)W & 15) == 0);
             k_partition_cap<MAS, HAS_W, false><<<nblk, kPartThreads, psm, ctx->stream>>>(
                 pos, W, nullptr, 0u, n, b1, w1, capC, ccur, inv, g, bulk_in, sp, spw, spill_n,
