@@ -721,8 +721,10 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
     float *sw2 = sp2 + 3 * KP;
     unsigned short *skey = reinterpret_cast<unsigned short *>(sw2 + WS);
     unsigned short *skey2 = skey + KP;
-    unsigned *hist = reinterpret_cast<unsigned *>(skey2 + KP);   // kMaxKeys each
-    unsigned *gdiff = hist + kMaxKeys;   // slot of key-ordered element e: gdiff[key] + e
+    // key histograms, one per chunk parity (a chunk's histogram is cleared
+    // after its scan, two barriers before the chunk after next uses it)
+    unsigned *histb = reinterpret_cast<unsigned *>(skey2 + KP);   // 2 * kMaxKeys
+    unsigned *gdiff = histb + 2 * kMaxKeys;   // slot of key-ordered element e: gdiff[key] + e
     unsigned *glim = gdiff + kMaxKeys;   // elements e < glim[key] fit their slots
     unsigned *gsp = glim + kMaxKeys;     // spill index of the others: gsp[key] + e
     unsigned *hex = gsp + kMaxKeys;      // each key's first position in key order
@@ -732,6 +734,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
     unsigned char *ctab = reinterpret_cast<unsigned char *>(mcnt + kMaxKeys);
     __shared__ unsigned s_warp[32];
     __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ int s_fail;               // a bulk-copy wait gave up
 
     // chunks: the input in KP pieces (coarse), or each bucket's particles in
     // KP pieces (fine; cpre = exclusive prefix of the chunks per bucket)
@@ -800,8 +803,9 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         mbar_init(&s_bar[0], 1);
         mbar_init(&s_bar[1], 1);
         mbar_init_fence();
+        s_fail = 0;
     }
-    for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;
+    for (int k = threadIdx.x; k < 2 * kMaxKeys; k += blockDim.x) histb[k] = 0u;
     __syncthreads();   // (also publishes the fine pass's chunk table)
     unsigned parity = 0u, pend = 0u;
     long long r0;
@@ -859,25 +863,27 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         }
         float *sp = sm + 3 * KP * b;
         float *sw = sm + 6 * KP + WS * b;
-        if (pend & (1u << b)) {
-            const unsigned ph = (parity >> b) & 1u;
-            const bool ok = mbar_wait_parity(&s_bar[b], ph);
+        unsigned *hist = histb + kMaxKeys * b;
+        // Each thread waits for the bulk copy itself (its completed wait
+        // makes the copied data visible to it) and goes on to the key phase;
+        // a wait that gave up is reported through s_fail and the whole CTA
+        // leaves after the next barrier.
+        const bool was_bulk = (pend & (1u << b)) != 0;
+        const unsigned ph = (parity >> b) & 1u;
+        bool ok = true;
+        if (was_bulk) {
+            ok = mbar_wait_parity(&s_bar[b], ph);
             parity ^= 1u << b;
             pend &= ~(1u << b);
-            if (__syncthreads_or(!ok)) {
-                if (threadIdx.x == 0) atomicOr(status, kStatusWaitTimeout);
-                mbar_wait_parity(&s_bar[b], ph);
-                if (pend) mbar_wait_parity(&s_bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
-                return;
-            }
+            if (!ok) s_fail = 1;
         } else {
             for (int j = threadIdx.x; j < 3 * cnt; j += blockDim.x) sp[j] = __ldcs(src + 3 * r0 + j);
             if (HAS_W)
                 for (int j = threadIdx.x; j < cnt; j += blockDim.x) sw[j] = __ldcs(srcw + r0 + j);
             __syncthreads();
         }
-        // (hist is zero here: cleared before the loop and after the
-        // previous chunk's scan)
+        // (hist is zero here: cleared before the loop and after the scan of
+        // the chunk before the previous one)
         // each thread's PT particles stay in registers from here to the
         // counting sort, with their key and their rank within the key (the
         // histogram atomic's old value)
@@ -915,11 +921,25 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
                 }
             }
         };
-        if (cnt == KP) key_phase(std::true_type());
-        else key_phase(std::false_type());
+        if (!ok) {
+#pragma unroll
+            for (int u = 0; u < PT; ++u) pk[u] = -1;   // nothing of this chunk is read
+        } else if (cnt == KP) {
+            key_phase(std::true_type());
+        } else {
+            key_phase(std::false_type());
+        }
         // (the barrier also tells whether any run of the previous chunk
         // overflowed its slots)
         const bool spilled = __syncthreads_or(my_spill) != 0;
+        if (s_fail) {
+            // a bulk-copy wait gave up: wait (bounded) for the copies still
+            // in flight into this CTA's buffers, then leave
+            if (threadIdx.x == 0) atomicOr(status, kStatusWaitTimeout);
+            if (was_bulk && !ok) mbar_wait_parity(&s_bar[b], ph);
+            if (pend) mbar_wait_parity(&s_bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+            return;
+        }
         const unsigned hv = threadIdx.x < nkeys ? hist[threadIdx.x] : 0u;
         // reserve the key's run now; its value is first needed after the
         // counting sort, so the atomic's round trip overlaps the previous
@@ -967,7 +987,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         __syncthreads();
         // every read of this chunk's histogram and of the previous chunk's
         // key-ordered buffer and tables is behind the barrier
-        for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;   // next chunk
+        for (int k = threadIdx.x; k < kMaxKeys; k += blockDim.x) hist[k] = 0u;   // chunk after next
 #pragma unroll
         for (int u = 0; u < PT; ++u) {
             if (pk[u] >= 0) {
@@ -1590,11 +1610,12 @@ size_t partition_smem(bool weighted) {
            sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * 5 * kMaxKeys;
 }
 
-// k_partition_cap: the same buffers, five per-key tables, the bucket chunk
-// prefix and counts and the fine pass's chunk -> bucket table
+// k_partition_cap: the same buffers, two key histograms, four per-key
+// tables, the bucket chunk prefix and counts and the fine pass's chunk ->
+// bucket table
 size_t partition_cap_smem(bool weighted) {
     return sizeof(float) * (9 * (size_t)KP + (weighted ? 3 * (size_t)KP : 0)) +
-           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (7 * kMaxKeys + 1) +
+           sizeof(unsigned short) * 2 * (size_t)KP + sizeof(unsigned) * (8 * kMaxKeys + 1) +
            kChunkTab;
 }
 
