@@ -280,6 +280,12 @@ __device__ __forceinline__ int wrap_cell(int i, const TileGeom &g) {
     return g.dmask >= 0 ? (i & g.dmask) : wrap_idx(i, g.dims);
 }
 
+// The same with the grid's kind known at compile time (P2: power of two).
+template <class P2>
+__device__ __forceinline__ int wrap_as(P2, int i, const TileGeom &g) {
+    return P2::value ? (i & g.dmask) : wrap_idx(i, g.dims);
+}
+
 // Partition shape (compile-time; the defaults are the measured best):
 // particles staged per chunk, threads per CTA (>= kMaxKeys: one scan value
 // per thread), resident CTAs per SM the registers are sized for.  2048
@@ -1243,10 +1249,10 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             // home cell, and from it (or from box sums) the scale
             int lmi = 0;       // largest count this thread has seen
             float lmf = 0.f;   // ... or largest sum of |W| (a NaN sticks)
-            auto occupy = [&](float x, float y, float z, float w) {
-                const int hx = wrap_cell(home_cell<MAS>(cell_dist(x, inv)), g);
-                const int hy = wrap_cell(home_cell<MAS>(cell_dist(y, inv)), g);
-                const int hz = wrap_cell(home_cell<MAS>(cell_dist(z, inv)), g);
+            auto occupy = [&](auto p2, float x, float y, float z, float w) {
+                const int hx = wrap_as(p2, home_cell<MAS>(cell_dist(x, inv)), g);
+                const int hy = wrap_as(p2, home_cell<MAS>(cell_dist(y, inv)), g);
+                const int hz = wrap_as(p2, home_cell<MAS>(cell_dist(z, inv)), g);
                 const int c = ((hx - ox + S::LO) * RY + (hy - oy + S::LO)) * RZ + (hz - oz + S::LO);
                 if (HAS_W) {
                     const float o = atomicAdd(&s_reg[c], fabsf(w)) + fabsf(w);
@@ -1255,7 +1261,9 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                     lmi = max(lmi, atomicAdd(&s_int[c], 1) + 1);
                 }
             };
-            // two particles per thread and step, both loaded first
+            // two particles per thread and step, both loaded first; the
+            // grid's wrap chosen once per item
+            auto occupy_all = [&](auto p2) {
             for (long long i = p0 + threadIdx.x; i < p1; i += 2 * blockDim.x) {
                 const long long i2 = i + blockDim.x;
                 const float x = __ldg(spos + 3 * i), y = __ldg(spos + 3 * i + 1),
@@ -1268,9 +1276,12 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                     z2 = __ldg(spos + 3 * i2 + 2);
                     if (HAS_W) w2 = __ldg(sw + i2);
                 }
-                occupy(x, y, z, w);
-                if (i2 < p1) occupy(x2, y2, z2, w2);
+                occupy(p2, x, y, z, w);
+                if (i2 < p1) occupy(p2, x2, y2, z2, w2);
             }
+            };
+            if (g.dmask >= 0) occupy_all(std::true_type());
+            else occupy_all(std::false_type());
             // A footprint cell takes taps from the home cells of an R^3 box
             // only, so R^3 times the largest home cell bounds every cell.
             // Where that bound leaves fewer than FAST_BITS fractional bits,
@@ -1311,13 +1322,16 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 exact_mass = MIN_BITS < 20 && e < 20;
             }
         }
-        auto deposit_one = [&](float px, float py, float pz, float wt) {
+        // one particle: P2 -- power-of-two grid (mask wrap); M -- 0 fixed point,
+        // 1 fixed point with mass-exact rounding, 2 float / compensated
+        auto deposit_one = [&](auto p2, auto mode, float px, float py, float pz, float wt) {
+            constexpr int M = decltype(mode)::value;
             int lx[NT], ly[NT], lz[NT];
             float wx[NT], wy[NT], wz[NT];
             {
                 const float d = cell_dist(px, inv);
                 const int c = home_cell<MAS>(d);
-                const int base = wrap_cell(c, g) - ox + S::LO;
+                const int base = wrap_as(p2, c, g) - ox + S::LO;
                 int o[NT];
                 axis_stencil<MAS>(d, c, o, wx);
 #pragma unroll
@@ -1326,7 +1340,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             {
                 const float d = cell_dist(py, inv);
                 const int c = home_cell<MAS>(d);
-                const int base = wrap_cell(c, g) - oy + S::LO;
+                const int base = wrap_as(p2, c, g) - oy + S::LO;
                 int o[NT];
                 axis_stencil<MAS>(d, c, o, wy);
 #pragma unroll
@@ -1335,19 +1349,19 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             {
                 const float d = cell_dist(pz, inv);
                 const int c = home_cell<MAS>(d);
-                const int base = wrap_cell(c, g) - oz + S::LO;
+                const int base = wrap_as(p2, c, g) - oz + S::LO;
                 int o[NT];
                 axis_stencil<MAS>(d, c, o, wz);
 #pragma unroll
                 for (int j = 0; j < NT; ++j) lz[j] = base + o[j];
             }
-            if (FIXED && fixed) {
+            if (M < 2) {
                 // Each tap rounded to the item's fixed point.  In items whose
                 // scale is coarse (dense clumps, 2^e < 2^20), the particle's
                 // rounding residue -- its quantized mass minus the sum of its
                 // quantized taps -- also goes to its largest tap, so that the
                 // many tiny outer taps rounding to zero cannot bias the mass.
-                if (MIN_BITS >= 20 || !exact_mass) {
+                if (M == 0) {
                     // the scale (a power of two) folded into the x weights:
                     // the same products, exactly, with NT^3 fewer multiplies
                     float wxs[NT];
@@ -1422,7 +1436,9 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 }
             }
         };
-        // two particles per thread and step, both loaded first
+        // two particles per thread and step, both loaded first; the form
+        // of the item and the grid's wrap chosen once per item
+        auto deposit_all = [&](auto p2, auto mode) {
         for (long long i = p0 + threadIdx.x; i < p1; i += 2 * blockDim.x) {
             const long long i2 = i + blockDim.x;
             const float x = __ldcs(spos + 3 * i), y = __ldcs(spos + 3 * i + 1),
@@ -1435,8 +1451,20 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 z2 = __ldcs(spos + 3 * i2 + 2);
                 if (HAS_W) w2 = __ldcs(sw + i2);
             }
-            deposit_one(x, y, z, w);
-            if (i2 < p1) deposit_one(x2, y2, z2, w2);
+            deposit_one(p2, mode, x, y, z, w);
+            if (i2 < p1) deposit_one(p2, mode, x2, y2, z2, w2);
+        }
+        };
+        using Fix = std::integral_constant<int, 0>;
+        using FixMass = std::integral_constant<int, 1>;
+        using Flt = std::integral_constant<int, 2>;
+        if (FIXED && fixed && (MIN_BITS >= 20 || !exact_mass)) {
+            if (g.dmask >= 0) deposit_all(std::true_type(), Fix());
+            else deposit_all(std::false_type(), Fix());
+        } else if (FIXED && fixed) {
+            deposit_all(std::false_type(), FixMass());
+        } else {
+            deposit_all(std::false_type(), Flt());
         }
         __syncthreads();
         // footprint cell value as a float
