@@ -316,6 +316,16 @@ __device__ __forceinline__ int tile_of(float x, float y, float z, float inv, con
     return ((hx >> g.sx) * g.nty + (hy >> g.sy)) * g.ntz + (hz >> g.sz);
 }
 
+// The same with the grid's kind known at compile time (P2: power of two).
+template <int MAS, class P2>
+__device__ __forceinline__ int tile_of_as(P2 p2, float x, float y, float z, float inv,
+                                          const TileGeom &g) {
+    const int hx = wrap_as(p2, home_cell<MAS>(cell_dist(x, inv)), g);
+    const int hy = wrap_as(p2, home_cell<MAS>(cell_dist(y, inv)), g);
+    const int hz = wrap_as(p2, home_cell<MAS>(cell_dist(z, inv)), g);
+    return ((hx >> g.sx) * g.nty + (hy >> g.sy)) * g.ntz + (hz >> g.sz);
+}
+
 // Counting pass: particles per tile (shared histogram, then global adds).
 // It also counts tile changes between neighbouring particles of each warp
 // (particle i vs i-1): few changes mean the input order is already spatially
@@ -902,7 +912,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
         unsigned pr[PT];
         // (a whole chunk, the common case, takes the loop without the
         // per-particle bounds test)
-        auto key_phase = [&](auto whole) {
+        auto key_phase = [&](auto whole, auto p2) {
 #pragma unroll
             for (int q4 = 0; q4 < PT / 4; ++q4) {
                 const int i0 = PT * threadIdx.x + 4 * q4;
@@ -920,7 +930,7 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
                         py[u] = ys[v];
                         pz[u] = zs[v];
                         if (HAS_W) pw[u] = sw[i0 + v];
-                        const int t = tile_of<MAS>(px[u], py[u], pz[u], inv, g);
+                        const int t = tile_of_as<MAS>(p2, px[u], py[u], pz[u], inv, g);
                         pk[u] = FINE ? t - keybase : t >> g.sF;
                         pr[u] = atomicAdd(&hist[pk[u]], 1u);
                     }
@@ -931,9 +941,10 @@ k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
 #pragma unroll
             for (int u = 0; u < PT; ++u) pk[u] = -1;   // nothing of this chunk is read
         } else if (cnt == KP) {
-            key_phase(std::true_type());
+            if (g.dmask >= 0) key_phase(std::true_type(), std::true_type());
+            else key_phase(std::true_type(), std::false_type());
         } else {
-            key_phase(std::false_type());
+            key_phase(std::false_type(), std::false_type());
         }
         // (the barrier also tells whether any run of the previous chunk
         // overflowed its slots)
