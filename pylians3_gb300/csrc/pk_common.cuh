@@ -80,6 +80,28 @@ __device__ __forceinline__ void mode_extras(Hist &H, const PkAcc &acc, int n2, i
     }
 }
 
+// Adds a run's moments to bin b of a CTA histogram (float shared atomics: the
+// warps of a CTA share it).
+template <class Hist>
+__device__ __forceinline__ void hist_add3(Hist &H, int b, float c0, float c1, float c2) {
+    atomicAdd(&H.h3[3 * b + 0], c0);
+    atomicAdd(&H.h3[3 * b + 1], c1);
+    atomicAdd(&H.h3[3 * b + 2], c2);
+}
+
+// A histogram private to one warp whose flushed runs never share a bin (the
+// warp's modes have monotone |k|): plain read-modify-writes.
+struct WarpHist {
+    float *h3;
+};
+template <>
+__device__ __forceinline__ void hist_add3<WarpHist>(WarpHist &H, int b, float c0, float c1,
+                                                    float c2) {
+    H.h3[3 * b + 0] += c0;
+    H.h3[3 * b + 1] += c1;
+    H.h3[3 * b + 2] += c2;
+}
+
 // Runs of consecutive modes of one lane that fall into the same |k| bin:
 // the sums of the current run are kept in registers.  A bin's three sums
 // are the moments S0 = sum |delta|^2, S1 = sum |delta|^2 mu^2 and S2 = sum
@@ -100,9 +122,7 @@ struct RunAcc {
                     hb = cb;
                     h0 = c0; h1 = c1; h2 = c2;
                 } else {
-                    atomicAdd(&H.h3[3 * cb + 0], c0);
-                    atomicAdd(&H.h3[3 * cb + 1], c1);
-                    atomicAdd(&H.h3[3 * cb + 2], c2);
+                    hist_add3(H, cb, c0, c1, c2);
                 }
             }
             cb = b;
@@ -161,15 +181,10 @@ __device__ __forceinline__ void warp_flush_runs(Hist &H, const RunAcc &R) {
             v1 += n1;
             v2 += n2;
         }
-        atomicAdd(&H.h3[3 * R.cb + 0], v0);
-        atomicAdd(&H.h3[3 * R.cb + 1], v1);
-        atomicAdd(&H.h3[3 * R.cb + 2], v2);
+        hist_add3(H, R.cb, v0, v1, v2);
     }
-    if (R.hb >= 0 && !(lane > 0 && R.hb == prev_tb)) {
-        atomicAdd(&H.h3[3 * R.hb + 0], R.h0);
-        atomicAdd(&H.h3[3 * R.hb + 1], R.h1);
-        atomicAdd(&H.h3[3 * R.hb + 2], R.h2);
-    }
+    __syncwarp(FULL);
+    if (R.hb >= 0 && !(lane > 0 && R.hb == prev_tb)) hist_add3(H, R.hb, R.h0, R.h1, R.h2);
 }
 
 // L consecutive modes kxx0 .. kxx0+L-1 of one pencil (ky, kz fixed), read
