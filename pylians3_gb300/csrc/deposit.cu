@@ -1199,8 +1199,16 @@ __device__ __forceinline__ bool fixed_exponent(float m, int &e) {
 // with cap_count (the count-free sort) the fixed grid of ntiles * ipt items
 // (tile it / ipt, chunk it % ipt) over the tile slots of capT particles,
 // tile t holding min(cap_count[t], capT) of them.
+// Resident CTAs per SM the registers are held to: three for NGP / CIC
+// (their footprints fit three to an SM), two for TSC / PCS and the
+// compensated form (whose taps need up to 64 registers).
+template <int MAS, int ACC>
+constexpr int deposit_min_blocks() {
+    return (ACC != kAccComp && (MAS == PYL_MAS_NGP || MAS == PYL_MAS_CIC)) ? 3 : 2;
+}
+
 template <int MAS, bool HAS_W, int ACC>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, deposit_min_blocks<MAS, ACC>())
 k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                const unsigned *__restrict__ start, const uint2 *__restrict__ items,
                const unsigned *__restrict__ nitems, float inv, TileGeom g,
@@ -1227,8 +1235,14 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
     constexpr int MIN_BITS = MAS == PYL_MAS_PCS ? 24 : 0;
     using S = Stencil<MAS>;
     constexpr int NT = S::NT;
-    extern __shared__ float s_reg[];
+    extern __shared__ __align__(16) float s_reg[];
     int *s_int = reinterpret_cast<int *>(s_reg);
+    // zeroes the first nf floats of the footprint (16-byte stores)
+    auto zero_fp = [&](int nf) {
+        float4 *s4 = reinterpret_cast<float4 *>(s_reg);
+        for (int i = threadIdx.x; i < nf / 4; i += blockDim.x) s4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = (nf & ~3) + threadIdx.x; i < nf; i += blockDim.x) s_reg[i] = 0.f;
+    };
     __shared__ float s_max[32];
     const int RX = g.RX, RY = g.RY, RZ = g.RZ;
     const int cells = RX * RY * RZ;
@@ -1248,7 +1262,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             p0 = (long long)start[t] + (long long)item.y * kItemCap;
             p1 = min((long long)start[t + 1], p0 + (long long)kItemCap);
         }
-        for (int i = threadIdx.x; i < (COMP ? 2 : 1) * cells; i += blockDim.x) s_reg[i] = 0.f;
+        zero_fp((COMP ? 2 : 1) * cells);
         const int tx = t / (g.nty * g.ntz), ty = (t / g.ntz) % g.nty, tz = t % g.ntz;
         const int ox = tx * g.TX, oy = ty * g.TY, oz = tz * g.TZ;   // tile origin (cells)
         __syncthreads();
@@ -1325,7 +1339,7 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
                 fixed = fixed_exponent<MAS, HAS_W>(block_max_nan(m, s_max), e);
             }
             if (e < MIN_BITS) fixed = false;   // too coarse: float for this item
-            for (int i = threadIdx.x; i < cells; i += blockDim.x) s_int[i] = 0;
+            zero_fp(cells);
             __syncthreads();
             if (fixed) {
                 scale = ldexpf(1.f, e);
@@ -1503,23 +1517,38 @@ k_tile_deposit(const float *__restrict__ spos, const float *__restrict__ sw,
             const int q1 = (zs + RZ - 1 >= 0 ? zs + RZ - 1 : zs + RZ - 4) / 4;
             const int nq = q1 - q0 + 1;
             const int work = RX * RY * nq;
+            // quad w = (lx * RY + ly) * nq + q; each step advances w by
+            // blockDim.x, carried through (q, ly, lx) without divisions
+            int q = threadIdx.x % nq, ly, lx;
+            {
+                const int r = threadIdx.x / nq;
+                ly = r % RY;
+                lx = r / RY;
+            }
+            const int sq = blockDim.x % nq, sr = blockDim.x / nq;
+            const int sly = sr % RY, slx = sr / RY;
             for (int w = threadIdx.x; w < work; w += blockDim.x) {
-                const int q = w % nq;
-                const int r = w / nq;
-                const int ly = r % RY, lx = r / RY;
                 const int zq = 4 * (q0 + q);                      // unwrapped quad start
+                const int row = (lx * RY + ly) * RZ;
                 float v[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int lz = zq + e - zs;
-                    v[e] = (lz >= 0 && lz < RZ) ? cell((lx * RY + ly) * RZ + lz) : 0.f;
+                    v[e] = (lz >= 0 && lz < RZ) ? cell(row + lz) : 0.f;
                 }
                 if (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f) {
-                    const int gx = wrap_idx(ox - S::LO + lx, d);
-                    const int gy = wrap_idx(oy - S::LO + ly, d);
-                    const int gz = wrap_idx(zq, d);
+                    const int gx = wrap_cell(ox - S::LO + lx, g);
+                    const int gy = wrap_cell(oy - S::LO + ly, g);
+                    const int gz = wrap_cell(zq, g);
                     red_v4(grid + gx * dd + (long long)gy * d + gz, v[0], v[1], v[2], v[3]);
                 }
+                q += sq;
+                int carry = 0;
+                if (q >= nq) { q -= nq; carry = 1; }
+                ly += sly + carry;
+                carry = 0;
+                if (ly >= RY) { ly -= RY; carry = 1; }
+                lx += slx + carry;
             }
         } else {
             for (int c = threadIdx.x; c < cells; c += blockDim.x) {
