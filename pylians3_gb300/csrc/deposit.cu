@@ -717,7 +717,12 @@ k_partition(const float *__restrict__ src, const float *__restrict__ srcw,
 // global-atomic deposit adds to the grid.  Chunks never straddle buckets.
 // Otherwise as k_partition: persistent CTAs, the next chunk fetched by a
 // bulk copy while the current one is partitioned (bounded mbarrier waits),
-// a shared counting sort, each key's run written contiguously.
+// a shared counting sort, each key's run written contiguously.  Software
+// pipelined over chunks: a chunk's key-ordered particles are written out
+// during the next chunk, after that chunk's key phase, so each chunk's slot
+// reservations (one global atomic per key) return while the previous chunk
+// is written, its keys are scanned and its particles sorted; a chunk costs
+// two CTA barriers (after its key phase, after its scan).
 template <int MAS, bool HAS_W, bool FINE>
 __global__ void __launch_bounds__(kPartThreads, PYL_PART_MINB)
 k_partition_cap(const float *__restrict__ src, const float *__restrict__ srcw,
