@@ -88,9 +88,12 @@ constexpr bool pair_binning() {
     return ColsCfg<N>::THREADS >= 32 * ColsCfg<N>::C && ColsCfg<N>::C >= 8 && N % 64 == 0;
 }
 
-// Fused x transform + binning of the 3D sums by mirrored pairs.  The modes
-// at +kx and -kx of a pencil (ky, kz fixed) share |k|, its bin and mu^2 (and
-// the window), so warp w bins column w of the item alone: lane l takes |kx|
+// Fused x transform + binning of the 3D sums by mirrored pairs (the mode
+// loop of class Pk, library/Pk_library/Pk_library.pyx:311-378, for the 3D
+// multipoles: the same half-space selection :324-327, exact integer bins,
+// window and mu^2 as bin_run).  The modes at +kx and -kx of a pencil (ky, kz
+// fixed) share |k|, its bin and mu^2 (and the window), so warp w bins column
+// w of the item alone: lane l takes |kx|
 // in [L l, L l + L) (L = N / 64) and adds |v(+kx)|^2 + |v(-kx)|^2 with one
 // bin and mu^2 evaluation; lane 31 also takes |kx| = N/2 (no mirror), and
 // |kx| = 0 has none either.  On the half-space planes kz = 0 and kz = N/2
